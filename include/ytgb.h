@@ -1,0 +1,191 @@
+/*
+ * ytgb.h -- C ABI of the GB300 ray-casting sampler library (libytgb.so).
+ *
+ * The library replaces the native layer under yt's ImageSampler call surface
+ * (yt/utilities/lib/image_samplers.pyx): the per-brick Cython loop
+ * cast_through_kdtree + walk_volume + sampler callbacks becomes one CUDA
+ * launch over every brick of a view.  Every entry point is plain C: pointers,
+ * sizes, an int status (0 = ok, < 0 = error, message in ytgb_last_error()).
+ * Device pointers are owned by the caller (e.g. torch tensors); the library
+ * allocates no device memory.  `stream` is a cudaStream_t passed as void*.
+ */
+#ifndef YTGB_H
+#define YTGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YTGB_ABI_VERSION 1
+
+#define YTGB_OK 0
+#define YTGB_ERR_INVALID (-1)   /* bad argument, detected on the host */
+#define YTGB_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define YTGB_ERR_DEVICE (-3)    /* a device-side guard tripped (see error word) */
+
+/* sampler kinds: VolumeRenderSampler (image_samplers.pyx:405-487),
+ * ProjectionSampler (:327-343), InterpolatedProjectionSampler (:346-403) and
+ * the MIP sampler (ProjectionSampler with max; no reference counterpart). */
+#define YTGB_VOLUME_RENDER 0
+#define YTGB_PROJECTION 1
+#define YTGB_INTERPOLATED_PROJECTION 2
+#define YTGB_MIP 3
+
+/* ray generation: generate_vector_info_plane_parallel (lenses.pyx:179-192)
+ * or generate_vector_info_null, i.e. per-pixel arrays (lenses.pyx:196-207) */
+#define YTGB_LENS_PLANE_PARALLEL 0
+#define YTGB_LENS_PER_PIXEL 1
+
+/* pixel culling: calculate_extent_plane_parallel / _perspective / _null
+ * (lenses.pyx:22-55, :60-161, :169-175) */
+#define YTGB_EXTENT_PLANE_PARALLEL 0
+#define YTGB_EXTENT_PERSPECTIVE 1
+#define YTGB_EXTENT_NULL 2
+
+/* render flags */
+#define YTGB_FLAG_NO_COMPENSATION 1u   /* plain FP32 accumulation (precision study) */
+
+/* One brick: the fields of yt's VolumeContainer (volume_container.pxd:13-33,
+ * filled by PartitionedGrid.__cinit__, partitioned_grid.pyx:28-63).  The
+ * brick's field f occupies data[data_offset + f*field_stride ...] in the
+ * float32 arena: (dims+1)^3 vertex values for vertex-centred samplers, dims^3
+ * cell values for ProjectionSampler / MIP, C order. */
+typedef struct ytgb_brick {
+    double left_edge[3];
+    double right_edge[3];
+    double dds[3];        /* (right_edge - left_edge) / dims */
+    double idds[3];       /* 1 / dds */
+    int32_t dims[3];
+    int32_t n_fields;
+    int64_t data_offset;  /* float index of field 0 */
+    int64_t field_stride; /* floats between consecutive fields */
+    int64_t mask_offset;  /* byte index into the mask arena; -1 = all ones */
+    int64_t pad;
+} ytgb_brick;
+
+/* One view: the ray-generation and culling fields of ImageSampler
+ * (image_samplers.pxd:38-70, set in ImageSampler.__init__ :59-131). */
+typedef struct ytgb_view {
+    int32_t nx, ny;           /* image.shape[0], image.shape[1] (nv) */
+    int32_t lens;             /* YTGB_LENS_* */
+    int32_t extent;           /* YTGB_EXTENT_* */
+    double vp_pos[12];        /* plane-parallel: inv_mat.ravel('F') + back_center */
+    double vp_dir[3];         /* plane-parallel: normal * width[2] */
+    double center[3];
+    double bounds[4];
+    double x_vec[3];
+    double y_vec[3];
+    double width[3];
+    double camera_data[15];   /* position, width, east, north, normal */
+    double pdx, pdy;          /* (bounds[1]-bounds[0])/nx, (bounds[3]-bounds[2])/ny */
+    const double *px_pos;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
+    const double *px_dir;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
+} ytgb_view;
+
+/* Transfer function, packed for the device by ytgb_tf_pack from yt's
+ * FieldInterpolationTable set (field_interpolation_tables.pxd:27-61 and the
+ * VolumeRenderAccumulator of image_samplers.pyx:45-55). */
+#define YTGB_TF_MAX_TABLES 6
+#define YTGB_TF_MAX_BINS 4096
+typedef struct ytgb_tf {
+    int32_t n_fits;
+    int32_t grey_opacity;
+    int32_t nbins_max;
+    int32_t ctf_fast;                  /* 1: ColorTransferFunction layout */
+    int32_t field_table_ids[6];
+    int32_t field_id[6];
+    int32_t weight_field_id[6];
+    int32_t weight_table_id[6];
+    int32_t nbins[6];
+    float lo_excl[6];   /* largest float <= bounds[0]: v <= lo_excl -> 0 */
+    float hi_excl[6];   /* smallest float >= bounds[1]: v >= hi_excl -> 0 */
+    float b0[6];        /* bounds[0] as float, for the bin index */
+    float idbin[6];     /* 1/dbin as float, for the bin index */
+    /* table floats follow in a separate buffer: for table t, bin b:
+     * tab[(t*nbins_max + b)*4 + {0,1,2,3}] = {y, dy, d0_hi, d0_lo} */
+} ytgb_tf;
+
+/* Arguments of one render: cast_through_kdtree (image_samplers.pyx:146-197)
+ * for every brick of `order`, in that order, in one launch. */
+typedef struct ytgb_render_args {
+    int32_t kind;              /* YTGB_VOLUME_RENDER ... YTGB_MIP */
+    int32_t n_samples;         /* samples per cell (VR / interpolated projection) */
+    int32_t n_order;           /* number of entries in order / rects */
+    uint32_t flags;            /* YTGB_FLAG_* */
+    ytgb_view view;
+    const ytgb_brick *bricks;  /* device */
+    const int32_t *order;      /* device: brick indices in viewpoint order */
+    const int32_t *rects;      /* device: 4 per order entry, from ytgb_brick_rects */
+    const float *data;         /* device float32 arena */
+    const uint8_t *masks;      /* device mask arena, or NULL when all are -1 */
+    ytgb_tf tf;                /* by value, from ytgb_tf_pack (VR only) */
+    const float *tf_tables;    /* device, VR only */
+    double *image;             /* device (nx,ny,4) float64, updated in place */
+    const double *zbuffer;     /* device (nx,ny) float64, or NULL (all ones) */
+    unsigned long long *counters; /* device [4]: cell visits, ray-brick walks, rays, cells
+                                  * outside their brick (skipped); or NULL */
+    int32_t *error;            /* device error word (0 = ok), or NULL */
+} ytgb_render_args;
+
+/* ---- status -------------------------------------------------------------- */
+int ytgb_abi_version(void);
+const char *ytgb_last_error(void);
+/* reads and clears the device error word written by a render */
+int ytgb_check_error(const int32_t *d_error, void *stream);
+
+/* ---- host: pixel culling ------------------------------------------------- */
+/* Replaces ImageSampler.extent_function + the +-1 padding and clipping of
+ * cast_through_kdtree (image_samplers.pyx:159-163; lenses.pyx:22-175).
+ * For each brick order[k] writes rects[4k..4k+3] = {x0, x1, y0, y1}: the
+ * half-open pixel range [x0,x1) x [y0,y1) the reference would loop over.
+ * `bricks` and `order` are host arrays. */
+int ytgb_brick_rects(const ytgb_view *view, const ytgb_brick *bricks, int32_t n_bricks,
+                     const int32_t *order, int32_t n_order, int32_t *rects);
+
+/* ---- host: transfer function --------------------------------------------- */
+/* Replaces FIT_initialize_table (field_interpolation_tables.pxd:44-61) for the
+ * tables of VolumeRenderSampler.__cinit__ (image_samplers.pyx:425-447).
+ * values[t] points to nbins[t] float64 values; bounds is 2*n_fits.
+ * tables_out must hold n_fits * max(nbins) * 4 floats. */
+int ytgb_tf_pack(int32_t n_fits, const double *const *values, const int32_t *nbins,
+                 const double *bounds, const int32_t *field_ids, const int32_t *weight_field_ids,
+                 const int32_t *weight_table_ids, const int32_t *field_table_ids,
+                 int32_t grey_opacity, ytgb_tf *tf_out, float *tables_out);
+
+/* ---- device: rendering --------------------------------------------------- */
+/* One view over an ordered brick list; replaces the Python brick loop of
+ * KDTreeVolumeSource.render (render_source.py:594-596) calling
+ * ImageSampler.__call__ -> cast_through_kdtree -> walk_volume -> sample. */
+int ytgb_render(const ytgb_render_args *args, void *stream);
+
+/* Traversal trace: for every pixel, an FNV-1a hash over (brick, index[3],
+ * enter_t bits, exit_t bits) of every cell walk_volume (grid_traversal.pyx:
+ * 26-140) hands to the sampler, and the visit count.  hashes/counts are
+ * device (nx*ny) arrays, initialised by the caller (FNV offset basis, 0). */
+int ytgb_trace(const ytgb_render_args *args, unsigned long long *hashes, long long *counts, void *stream);
+
+/* ---- host: AMR kd-tree --------------------------------------------------- */
+/* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
+ * amr_kdtools.Node.add_grids / insert_grids / split_grids /
+ * kdtree_get_choices / divide (amr_kdtools.pyx:201-532, 760-823).
+ * Grids are added level by level in the given order. Returns a handle. */
+void *ytgb_kdtree_build(int32_t n_grids, const double *gles, const double *gres,
+                        const int64_t *gids, const int32_t *levels);
+void ytgb_kdtree_destroy(void *tree);
+/* number of leaves with a grid (the bricks) */
+int32_t ytgb_kdtree_num_leaves(void *tree);
+/* leaves in depth-first (left-first) order: kd_traverse() without viewpoint
+ * (amr_kdtools.pyx:102-107) */
+int ytgb_kdtree_leaves(void *tree, double *le, double *re, int64_t *grid_ids);
+/* leaf indices (into the depth-first list) in the viewpoint order of
+ * kd_traverse(viewpoint) (amr_kdtools.pyx:108-111, 612-622, 708-755) */
+int ytgb_kdtree_viewpoint_order(void *tree, const double *viewpoint, int32_t *order);
+/* the same for many viewpoints: order is n_views * num_leaves */
+int ytgb_kdtree_viewpoint_orders(void *tree, int32_t n_views, const double *viewpoints, int32_t *order);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* YTGB_H */

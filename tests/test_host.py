@@ -1,0 +1,170 @@
+"""Host-side pieces of libytgb against the oracle (no GPU needed)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import cpu as ocpu
+from oracle import glue
+from yt_gb300 import _lib, testing, workloads
+from yt_gb300.amr_kdtree import AMRKDTree, vertex_centred
+from yt_gb300.camera import Camera
+from yt_gb300.image_samplers import make_view
+from yt_gb300.transfer_functions import ColorTransferFunction, pack
+from yt_gb300.volume import BrickSet
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_library_exports_every_declared_symbol():
+    hdr = (ROOT / "include" / "ytgb.h").read_text()
+    names = set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(ytgb_\w+)\s*\(", hdr, flags=re.M))
+    assert len(names) >= 12
+    L = _lib.lib()
+    for n in sorted(names):
+        assert hasattr(L, n), n
+    assert set(_lib.SIGNATURES) == names
+
+
+CAMS = [
+    ((0.5, 0.5, -1.0), (1.0, 1.0, 1.0), 64, "plane-parallel"),
+    ((1.3, 0.2, -0.7), (1.0, 1.0, 1.0), (64, 50), "plane-parallel"),
+    ((-0.4, 1.1, 1.6), (0.7, 0.7, 0.7), 33, "plane-parallel"),
+    ((0.5, 0.5, -1.0), (1.5, 1.5, 1.5), 96, "perspective"),
+    ((1.6, 1.4, 1.9), (1.5, 1.5, 1.5), (80, 64), "perspective"),
+    ((0.45, 0.52, 0.55), (1.5, 1.5, 1.5), 48, "perspective"),
+]
+
+
+@pytest.mark.parametrize("pos,width,res,lens", CAMS)
+def test_camera_params_match_oracle(pos, width, res, lens):
+    a = Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens).sampler_params()
+    b = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens).sampler_params()
+    for k in ("vp_pos", "vp_dir", "center", "x_vec", "y_vec", "width", "camera_data"):
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+    assert tuple(a["bounds"]) == tuple(b["bounds"])
+    assert a["lens_type"] == b["lens_type"]
+
+
+@pytest.fixture(scope="module")
+def amr_small():
+    return workloads.amr_vr(root=32, levels=2, patch=8, res=64)
+
+
+@pytest.mark.parametrize("pos,width,res,lens", CAMS)
+def test_brick_rects_match_oracle(amr_small, pos, width, res, lens):
+    w = amr_small
+    cam = Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+    p = cam.sampler_params()
+    nx, ny = cam.resolution
+    view, _, _ = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"], p["y_vec"],
+                           p["width"], p["lens_type"], p["camera_data"])
+    bs = BrickSet(w.bricks, device="cpu")
+    order = w.order(cam)
+    rects = bs.rects(view, order)
+    s = ocpu.OracleSampler("volume_render", p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"],
+                           p["x_vec"], p["y_vec"], p["width"], lens_type=p["lens_type"],
+                           camera_data=p["camera_data"], tf=w.tf)
+    ob = ocpu.OracleBricks(w.bricks)
+    for k, b in enumerate(order):
+        assert np.array_equal(rects[k], s.padded_rect(ob, int(b))), k
+
+
+def test_vertex_centring_matches_oracle():
+    g = testing.blob_grid(18, seed=2)
+    assert np.array_equal(vertex_centred(g.data), ocpu.ghost_zone_vertex_centre(g.data))
+
+
+def test_kdtree_matches_oracle_restatement():
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=4)
+    kd = AMRKDTree(grids)
+    ot = glue.KDTree(grids)
+    leaves = ot.leaves()
+    assert kd.num_bricks == len(leaves)
+    for k, n in enumerate(leaves):
+        assert np.array_equal(kd.leaf_le[k], n.le) and np.array_equal(kd.leaf_re[k], n.re)
+        assert kd.leaf_grid[k] == n.grid
+    rng = np.random.default_rng(0)
+    for _ in range(6):
+        vp = rng.uniform(-1.0, 2.0, 3)
+        want = [(tuple(n.le), n.grid) for n in ot.leaves(vp)]
+        got = [(tuple(kd.leaf_le[k]), kd.leaf_grid[k]) for k in kd.viewpoint_order(vp)]
+        assert got == want
+    many = kd.viewpoint_orders(np.array([[0.1, 0.2, 3.0], [2.0, -1.0, 0.5]]))
+    assert np.array_equal(many[1], kd.viewpoint_order([2.0, -1.0, 0.5]))
+
+
+def test_bricks_match_oracle_slicing():
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=1)
+    kd = AMRKDTree(grids)
+    ot = glue.KDTree(grids)
+    byid = {g.id: g for g in grids}
+    vcd = {}
+    for k, node in enumerate(ot.leaves()):
+        g = byid[node.grid]
+        if g.id not in vcd:
+            vcd[g.id] = [glue.vertex_centred(g.data, True)]
+        want = glue.brick_data(node, g, vcd[g.id])
+        got = kd.brick(k)
+        np.testing.assert_array_equal(got[0][0], want[0][0])
+        assert np.array_equal(got[4], want[4])
+
+
+def test_tf_pack_ctf_layout():
+    tf = ColorTransferFunction((-0.2, 1.3), nbins=256)
+    for loc, w, rgba in testing.ctf_layers((-0.2, 1.3), 4):
+        tf.add_gaussian(loc, w, list(rgba))
+    pk = pack(tf)
+    h = pk.header
+    assert h.n_fits == 4 and h.ctf_fast == 1 and h.nbins_max == 256
+    assert list(h.weight_table_id)[:4] == [3, 3, 3, -1]
+    assert list(h.field_table_ids) == [0, 1, 2, 3, 0, 0]
+    # exclusive bounds: the float nearest outside each float64 bound
+    assert np.float32(h.lo_excl[0]) <= -0.2 and np.float64(np.nextafter(np.float32(h.lo_excl[0]), np.float32(1))) > -0.2
+    assert np.float32(h.hi_excl[0]) >= 1.3 and np.float64(np.nextafter(np.float32(h.hi_excl[0]), np.float32(-2))) < 1.3
+    tab = pk.tables.reshape(4, 256, 4)
+    y = tf.funcs[1].y
+    assert np.array_equal(tab[1, :, 0], y.astype(np.float32))
+    dbin = (1.3 - -0.2) / 255
+    d0 = -0.2 + np.arange(255) * dbin
+    assert np.allclose(tab[1, :255, 2].astype(np.float64) + tab[1, :255, 3], d0, rtol=0, atol=1e-14)
+
+
+def test_tf_pack_rejects_bad_input():
+    class Bad:
+        n_field_tables = 1
+        tables = [type("T", (), {"y": np.zeros(1), "x_bounds": (0.0, 1.0)})()]
+        field_ids = [0] * 6
+        weight_field_ids = [-1] * 6
+        weight_table_ids = [-1] * 6
+        field_table_ids = [0] * 6
+        grey_opacity = 0
+
+    with pytest.raises(_lib.YtgbError):
+        pack(Bad())
+
+
+def test_brick_rects_rejects_bad_order(amr_small):
+    w = amr_small
+    cam = w.views[0].camera
+    p = cam.sampler_params()
+    view, _, _ = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], 64, 64, p["x_vec"], p["y_vec"],
+                           p["width"], p["lens_type"], p["camera_data"])
+    bs = BrickSet(w.bricks[:3], device="cpu")
+    with pytest.raises(_lib.YtgbError):
+        bs.rects(view, np.array([0, 5], dtype=np.int32))
+
+
+def test_sampler_constructor_errors():
+    from yt_gb300.image_samplers import ProjectionSampler
+
+    img = np.zeros((4, 5, 4))
+    with pytest.raises(RuntimeError, match="Bad lens shape"):
+        ProjectionSampler(np.zeros((4, 4, 3)), np.zeros((4, 5, 3)), np.zeros(3), (0, 1, 0, 1), img, np.ones(3),
+                          np.ones(3), np.zeros(3), "KDTree", 1, lens_type="perspective")
+    s = ProjectionSampler(np.atleast_3d(np.zeros(12)), np.atleast_3d(np.ones(3)), np.zeros(3), (0, 1, 0, 1), img,
+                          np.ones(3), np.ones(3), np.ones(3), "Nope", 1, lens_type="plane-parallel")
+    with pytest.raises(NotImplementedError):
+        s(None)

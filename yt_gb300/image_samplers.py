@@ -1,0 +1,236 @@
+"""Drop-in replacements for yt's image samplers (yt/utilities/lib/image_samplers.pyx).
+
+``VolumeRenderSampler``, ``ProjectionSampler``,
+``InterpolatedProjectionSampler`` and the new ``MIPSampler`` take the same
+constructor arguments as yt's classes (``ImageSampler.__init__``
+:59-131, ``VolumeRenderSampler.__cinit__`` :406-446,
+``InterpolatedProjectionSampler.__cinit__`` :347-366) and the same call,
+``sampler(pg, num_threads=0)`` (:132-141), so yt's ``Scene`` /
+``KDTreeVolumeSource.render`` / ``off_axis_projection`` drive them unchanged.
+
+The difference is when the work happens.  yt casts every ray through each
+brick as the brick is passed in.  Here ``__call__`` only records the brick;
+the first read of ``aimage`` uploads all recorded bricks and renders them in
+ONE CUDA launch, in the order they were passed (yt passes them in kd
+viewpoint order), then writes the result into the caller's image array in
+place -- the same array yt's sampler would have mutated.  Reading ``aimage``
+is therefore the synchronisation point; ``flush()`` does the same
+explicitly.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import transfer_functions as _tfm
+from .volume import BrickSet, render as _render
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise _lib.YtgbError("yt_gb300 samplers need a CUDA device (there is no CPU fallback)")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def make_view(vp_pos, vp_dir, center, bounds, nx, ny, x_vec, y_vec, width, lens_type, camera_data):
+    """Build a ``ytgb_view`` from ImageSampler arguments.  Returns (view,
+    per-pixel positions or None, per-pixel directions or None)."""
+    v = _lib.View()
+    v.nx, v.ny = int(nx), int(ny)
+    vp_pos = np.asarray(vp_pos, dtype=np.float64)
+    vp_dir = np.asarray(vp_dir, dtype=np.float64)
+    px_pos = px_dir = None
+    if lens_type == "plane-parallel":
+        v.lens = _lib.LENS_PLANE_PARALLEL
+        v.extent = _lib.EXTENT_PLANE_PARALLEL
+        flat_p = vp_pos.ravel()
+        flat_d = vp_dir.ravel()
+        if flat_p.size != 12 or flat_d.size != 3:
+            raise RuntimeError("plane-parallel lens needs 12 position and 3 direction parameters")
+        for i in range(12):
+            v.vp_pos[i] = float(flat_p[i])
+        for i in range(3):
+            v.vp_dir[i] = float(flat_d[i])
+    else:
+        # image_samplers.pyx:90-96
+        if not (vp_pos.shape[0] == vp_dir.shape[0] == nx) or not (vp_pos.shape[1] == vp_dir.shape[1] == ny):
+            msg = f"Bad lens shape / direction for {lens_type}\n"
+            msg += "Shapes: ({} - {} - {}) and ({} - {} - {})".format(
+                vp_pos.shape[0], vp_dir.shape[0], nx, vp_pos.shape[1], vp_dir.shape[1], ny)
+            raise RuntimeError(msg)
+        v.lens = _lib.LENS_PER_PIXEL
+        if camera_data is not None and lens_type == "perspective":
+            v.extent = _lib.EXTENT_PERSPECTIVE
+        else:
+            v.extent = _lib.EXTENT_NULL
+        px_pos = np.ascontiguousarray(vp_pos.reshape(nx, ny, 3))
+        px_dir = np.ascontiguousarray(vp_dir.reshape(nx, ny, 3))
+    for i in range(3):
+        v.center[i] = float(center[i])
+        v.x_vec[i] = float(x_vec[i])
+        v.y_vec[i] = float(y_vec[i])
+        v.width[i] = float(width[i])
+    for i in range(4):
+        v.bounds[i] = float(bounds[i])
+    v.pdx = (v.bounds[1] - v.bounds[0]) / v.nx
+    v.pdy = (v.bounds[3] - v.bounds[2]) / v.ny
+    if camera_data is not None:
+        cd = np.asarray(camera_data, dtype=np.float64).ravel()
+        for i in range(15):
+            v.camera_data[i] = float(cd[i])
+    return v, px_pos, px_dir
+
+
+def brick_tuple(pg):
+    """(data, mask, left_edge, right_edge, dims) of a PartitionedGrid -- yt's
+    own Cython object or :class:`yt_gb300.partitioned_grid.PartitionedGrid`.
+    dims come from the mask, which has one entry per cell."""
+    data = list(pg.my_data)
+    mask = np.asarray(pg.source_mask)
+    dims = np.array(mask.shape, dtype=np.int64)
+    return data, mask, np.asarray(pg.LeftEdge, dtype=np.float64), np.asarray(pg.RightEdge, dtype=np.float64), dims
+
+
+class ImageSampler:
+    kind = None
+
+    def __init__(self, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, *args,
+                 **kwargs):
+        self.volume_method = volume_method
+        camera_data = kwargs.pop("camera_data", None)
+        if camera_data is not None:
+            self.camera_data = camera_data
+        zbuffer = kwargs.pop("zbuffer", None)
+        if zbuffer is None:
+            zbuffer = np.ones((image.shape[0], image.shape[1]), "float64")
+        self.lens_type = kwargs.pop("lens_type", None)
+        self.flags = int(kwargs.pop("flags", 0))
+        self._image = image
+        nx, ny = image.shape[0], image.shape[1]
+        self._view, self._px_pos, self._px_dir = make_view(
+            vp_pos, vp_dir, center, bounds, nx, ny, x_vec, y_vec, width, self.lens_type, camera_data)
+        self.acenter = center
+        self.ax_vec = x_vec
+        self.ay_vec = y_vec
+        self.azbuffer = np.asarray(zbuffer)
+        self.nv = (nx, ny)
+        self.bounds = tuple(float(b) for b in bounds)
+        self.pdx = (self.bounds[1] - self.bounds[0]) / nx
+        self.pdy = (self.bounds[3] - self.bounds[2]) / ny
+        self.width = np.array(width, dtype=np.float64)
+        self._pending = []
+        self.n_samples = 1
+        self.last_counters = None
+
+    # ---- the call surface ---------------------------------------------------
+    def __call__(self, pg, **kwa):
+        if self.volume_method == "KDTree":
+            return self.cast_through_kdtree(pg, **kwa)
+        elif self.volume_method == "Octree":
+            raise NotImplementedError(
+                'Volume rendering has not been implemented for method: "Octree" in yt_gb300')
+        else:
+            raise NotImplementedError(
+                f'Volume rendering has not been implemented for method: "{self.volume_method}"')
+
+    def cast_through_kdtree(self, pg, num_threads=0):
+        """Record the brick; it is rendered at the next ``aimage`` read."""
+        data = list(pg.my_data)
+        if len(data) > 6:
+            raise ValueError("at most 6 fields per brick are supported")
+        self._pending.append(pg)
+        return 0
+
+    @property
+    def aimage(self):
+        self.flush()
+        return self._image
+
+    @aimage.setter
+    def aimage(self, value):
+        self.flush()
+        self._image = value
+
+    @property
+    def image(self):
+        return self.aimage
+
+    # ---- execution ------------------------------------------------------------
+    def _tf(self):
+        return None
+
+    def flush(self):
+        if not self._pending:
+            return
+        pending, self._pending = self._pending, []
+        dev = _device()
+        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev)
+        order = np.arange(len(pending), dtype=np.int32)
+        img = np.ascontiguousarray(self._image, dtype=np.float64)
+        image_d = torch.from_numpy(img).to(dev)
+        zb = torch.from_numpy(np.ascontiguousarray(self.azbuffer, dtype=np.float64)).to(dev)
+        px_pos = px_dir = None
+        if self._px_pos is not None:
+            px_pos = torch.from_numpy(self._px_pos).to(dev)
+            px_dir = torch.from_numpy(self._px_dir).to(dev)
+        counters = torch.zeros(4, dtype=torch.int64, device=dev)
+        error = torch.zeros(1, dtype=torch.int32, device=dev)
+        _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb,
+                n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
+                px_pos=px_pos, px_dir=px_dir)
+        stream = torch.cuda.current_stream(dev)
+        _lib.check(_lib.lib().ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
+        out = image_d.cpu().numpy()
+        self._image[...] = out
+        self.last_counters = counters.cpu().numpy()
+
+    def ensure_code_unit_params(self, params):
+        for name in ["center", "vp_pos", "vp_dir", "width"]:
+            p = params[name]
+            if hasattr(p, "in_units"):
+                params[name] = p.in_units("code_length")
+        b = params["bounds"]
+        if hasattr(b[0], "units"):
+            params["bounds"] = tuple(x.in_units("code_length").d for x in b)
+        return params
+
+
+class ProjectionSampler(ImageSampler):
+    """Line integral of cell-centred data (image_samplers.pyx:327-343):
+    rgba[i] += data[i][cell] * (exit_t - enter_t), i < min(4, n_fields)."""
+    kind = _lib.PROJECTION
+
+
+class MIPSampler(ImageSampler):
+    """Maximum-intensity projection: ProjectionSampler with max in place of +=
+    (no counterpart in yt's ray caster)."""
+    kind = _lib.MIP
+
+
+class InterpolatedProjectionSampler(ImageSampler):
+    """Trilinear samples of vertex-centred data summed along the ray
+    (image_samplers.pyx:346-403)."""
+    kind = _lib.INTERPOLATED_PROJECTION
+
+    def __init__(self, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method,
+                 n_samples=10, **kwargs):
+        super().__init__(vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, **kwargs)
+        self.n_samples = int(n_samples)
+
+
+class VolumeRenderSampler(ImageSampler):
+    """Emission-absorption volume rendering through yt's transfer-function
+    tables (image_samplers.pyx:405-487)."""
+    kind = _lib.VOLUME_RENDER
+
+    def __init__(self, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, tf_obj,
+                 n_samples=10, **kwargs):
+        super().__init__(vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, **kwargs)
+        assert tf_obj.n_field_tables <= 6
+        self.tf_obj = tf_obj
+        self.n_samples = int(n_samples)
+        self._packed = _tfm.pack(tf_obj)
+
+    def _tf(self):
+        return self._packed
