@@ -116,6 +116,9 @@ def lib() -> C.CDLL:
         _lib.yo_ghost_zone_interpolate.restype = None
         _lib.yo_ghost_zone_interpolate.argtypes = [C.c_int, _dp, C.POINTER(C.c_int64), _dp, _dp,
                                                    C.POINTER(C.c_int64), _dp]
+        _lib.yo_trace_rays.restype = None
+        _lib.yo_trace_rays.argtypes = [C.POINTER(YoVC), _dp, _dp, _dp, C.c_int64, C.c_int64,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int32), _dp]
         assert _lib.yo_sizeof_sampler() == C.sizeof(YoSampler), "yo_sampler layout mismatch"
         assert _lib.yo_sizeof_vc() == C.sizeof(YoVC), "yo_vc layout mismatch"
     return _lib
@@ -259,3 +262,18 @@ def ghost_zone_vertex_centre(cell: np.ndarray) -> np.ndarray:
     lib().yo_ghost_zone_interpolate(1, _ptr(cell), _ptr(ish, C.c_int64), _ptr(il), _ptr(out),
                                     _ptr(osh, C.c_int64), _ptr(ol))
     return out
+
+
+def trace_rays(brick, pos, dirs, max_t, cap):
+    """walk_volume over arbitrary rays through one brick: (counts, cells, ts)."""
+    ob = OracleBricks([brick])
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float64)
+    max_t = np.ascontiguousarray(max_t, dtype=np.float64)
+    n = pos.shape[0]
+    counts = np.zeros(n, dtype=np.int64)
+    cells = np.zeros((n, cap, 3), dtype=np.int32)
+    ts = np.zeros((n, cap, 2), dtype=np.float64)
+    lib().yo_trace_rays(C.byref(ob.vcs[0]), _ptr(pos), _ptr(dirs), _ptr(max_t), n, cap,
+                        _ptr(counts, C.c_int64), _ptr(cells, C.c_int32), _ptr(ts))
+    return counts, cells, ts

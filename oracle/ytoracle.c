@@ -260,6 +260,16 @@ static inline void fit_eval_transfer(double dt, const double *dvs, double *rgba,
     }
 }
 
+/* The reference can pass an index outside the brick (an axis with v_dir == 0
+ * snapped onto a face from just outside starts at -1, grid_traversal.pyx:67-78
+ * and :113-117) and then reads outside its arrays.  Such cells contribute
+ * nothing here, as on the GPU. */
+static inline int yo_inside(const yo_vc *vc, const int index[3])
+{
+    return index[0] >= 0 && index[0] < vc->dims[0] && index[1] >= 0 && index[1] < vc->dims[1] &&
+           index[2] >= 0 && index[2] < vc->dims[2];
+}
+
 typedef struct {
     double rgba[4];
     const yo_sampler *s;
@@ -274,6 +284,7 @@ static void sample_vr(const yo_vc *vc, const double v_pos[3], const double v_dir
     int offset = index[0] * (vc->dims[1] + 1) * (vc->dims[2] + 1) + index[1] * (vc->dims[2] + 1) + index[2];
     int cell_offset = index[0] * (vc->dims[1]) * (vc->dims[2]) + index[1] * (vc->dims[2]) + index[2];
     double dp[3], ds[3], dt, dvs[6] = {0, 0, 0, 0, 0, 0};
+    if (!yo_inside(vc, index)) return;
     if (vc->mask[cell_offset] != 1) return;
     dt = (exit_t - enter_t) / s->n_samples;
     for (i = 0; i < 3; i++) {
@@ -297,6 +308,7 @@ static void sample_projection(const yo_vc *vc, const double v_pos[3], const doub
     double dl = (exit_t - enter_t);
     int di = (index[0] * vc->dims[1] + index[1]) * vc->dims[2] + index[2];
     (void)v_pos; (void)v_dir;
+    if (!yo_inside(vc, index)) return;
     for (i = 0; i < n; i++) im->rgba[i] += vc->data[i][di] * dl;
 }
 
@@ -307,6 +319,7 @@ static void sample_mip(const yo_vc *vc, const double v_pos[3], const double v_di
     int i, n = vc->n_fields < 4 ? vc->n_fields : 4;
     int di = (index[0] * vc->dims[1] + index[1]) * vc->dims[2] + index[2];
     (void)v_pos; (void)v_dir; (void)enter_t; (void)exit_t;
+    if (!yo_inside(vc, index)) return;
     for (i = 0; i < n; i++) {
         double v = vc->data[i][di];
         if (v > im->rgba[i]) im->rgba[i] = v;
@@ -322,6 +335,7 @@ static void sample_interp_proj(const yo_vc *vc, const double v_pos[3], const dou
     int offset = index[0] * (vc->dims[1] + 1) * (vc->dims[2] + 1) + index[1] * (vc->dims[2] + 1) + index[2];
     double dp[3], ds[3], dvs[6] = {0, 0, 0, 0, 0, 0};
     double dt = (exit_t - enter_t) / s->n_samples;
+    if (!yo_inside(vc, index)) return;
     for (i = 0; i < 3; i++) {
         dp[i] = (enter_t + 0.5 * dt) * v_dir[i] + v_pos[i];
         dp[i] -= index[i] * vc->dds[i] + vc->left_edge[i];
@@ -667,3 +681,41 @@ void yo_ghost_zone_interpolate(int rf, const double *in, const int64_t ishape[3]
 
 int yo_sizeof_sampler(void) { return (int)sizeof(yo_sampler); }
 int yo_sizeof_vc(void) { return (int)sizeof(yo_vc); }
+
+/* ---- per-ray traversal record (for comparison with the reference probe) -- */
+typedef struct {
+    int64_t n, cap;
+    int32_t *cells;
+    double *ts;
+} yo_rec;
+
+static void sample_record(const yo_vc *vc, const double v_pos[3], const double v_dir[3],
+                          double enter_t, double exit_t, const int index[3], void *data)
+{
+    yo_rec *r = (yo_rec *)data;
+    (void)vc; (void)v_pos; (void)v_dir;
+    if (r->n < r->cap) {
+        r->cells[3 * r->n + 0] = index[0];
+        r->cells[3 * r->n + 1] = index[1];
+        r->cells[3 * r->n + 2] = index[2];
+        r->ts[2 * r->n + 0] = enter_t;
+        r->ts[2 * r->n + 1] = exit_t;
+    }
+    r->n += 1;
+}
+
+/* walk_volume for n arbitrary rays through one brick, recording every cell */
+void yo_trace_rays(const yo_vc *vc, const double *pos, const double *dir, const double *max_t, int64_t n,
+                   int64_t cap, int64_t *counts, int32_t *cells, double *ts)
+{
+    int64_t i;
+    for (i = 0; i < n; i++) {
+        yo_rec r;
+        r.n = 0;
+        r.cap = cap;
+        r.cells = cells + 3 * cap * i;
+        r.ts = ts + 2 * cap * i;
+        yo_walk_volume(vc, pos + 3 * i, dir + 3 * i, sample_record, &r, NULL, max_t[i]);
+        counts[i] = r.n;
+    }
+}

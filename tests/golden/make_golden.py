@@ -1,0 +1,207 @@
+"""Generate the golden fixtures of tests/golden/ from yt's own compiled sampler.
+
+Run in a checkout where the reference's sources are available (the build
+recipe oracle/build_ref.py compiles them into oracle/_ref/pkg):
+
+    python oracle/build_ref.py && python tests/golden/make_golden.py
+
+Every fixture stores its inputs as well as the reference's outputs, so the
+tests do not depend on the synthetic generators staying bit-stable.
+
+* gz.npz        ghost_zone_interpolate (interpolators.pyx:177-226) on a 6x7x5
+                random array and on a linear field (exactly reproduced, as in
+                yt's own test_interpolators.py:107-150)
+* trace.npz     walk_volume (grid_traversal.pyx:26-140) cell sequences and
+                enter/exit t for 400 rays through an 8x6x7 brick, through
+                yt's compiled walk_volume via oracle/ref_trace.pyx
+* vr.npz        VolumeRenderSampler images: a 16^3 blob brick, 4-layer CTF,
+                three cameras (axis-aligned and oblique plane-parallel,
+                perspective), n_samples 1 and 3
+* proj.npz      ProjectionSampler (cell-centred) and
+                InterpolatedProjectionSampler (vertex-centred) images
+* kd.npz        AMRKDTree leaves and viewpoint orders (amr_kdtools.pyx
+                Node.add_grids / kd_traverse) for a small AMR hierarchy
+* amr_vr.npz    a full AMR render: bricks from the reference's kd tree and
+                vertex centring, rendered by the reference sampler in
+                viewpoint order through a perspective camera
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle" / "_ref" / "pkg"))
+
+from yt.utilities.lib import image_samplers as RIS  # noqa: E402
+from yt.utilities.lib.amr_kdtools import Node  # noqa: E402
+from yt.utilities.lib.interpolators import ghost_zone_interpolate  # noqa: E402
+from yt.utilities.lib.partitioned_grid import PartitionedGrid  # noqa: E402
+
+import ytref_trace  # noqa: E402
+from oracle import glue  # noqa: E402
+from yt_gb300 import testing  # noqa: E402
+
+
+def ref_vertex(cell):
+    out = np.zeros(tuple(s + 1 for s in cell.shape))
+    ghost_zone_interpolate(1, np.ascontiguousarray(cell, dtype=np.float64), np.array([0.5] * 3), out, np.zeros(3))
+    return out
+
+
+def gz():
+    rng = np.random.default_rng(11)
+    a = rng.random((6, 7, 5))
+    x, y, z = np.meshgrid(np.arange(6) + 0.5, np.arange(7) + 0.5, np.arange(5) + 0.5, indexing="ij")
+    lin = 2.0 * x - 3.0 * y + 0.5 * z + 1.0
+    np.savez_compressed(HERE / "gz.npz", a=a, a_out=ref_vertex(a), lin=lin, lin_out=ref_vertex(lin))
+
+
+def trace():
+    rng = np.random.default_rng(12)
+    le, re = np.array([0.1, 0.2, 0.15]), np.array([0.9, 0.8, 0.85])
+    dims = np.array([8, 6, 7], dtype=np.int64)
+    n = 400
+    pos = rng.uniform(-0.5, 1.5, (n, 3))
+    target = rng.uniform(0.1, 0.9, (n, 3))
+    dirs = (target - pos) * rng.uniform(1.0, 2.5, (n, 1))
+    # axis-parallel rays, rays on cell faces and through brick corners
+    for k in range(0, 60):
+        ax = k % 3
+        d = np.zeros(3)
+        d[ax] = (1.0 if k % 2 else -1.0) * 2.0
+        p = rng.uniform(0.1, 0.9, 3)
+        if k % 4 == 0:
+            o = (ax + 1) % 3
+            p[o] = le[o] + (re[o] - le[o]) * rng.integers(0, int(dims[o]) + 1) / dims[o]
+        p[ax] = -0.5 if d[ax] > 0 else 1.5
+        pos[k], dirs[k] = p, d
+    for k in range(60, 90):
+        c = np.array([le[0], re[1], le[2]]) if k % 2 else re.copy()
+        pos[k] = c - dirs[k]
+    max_t = np.where(rng.random(n) < 0.2, rng.uniform(0.2, 0.9, n), 1.0)
+    pg = PartitionedGrid(0, [np.zeros(tuple(dims + 1))], np.ones(tuple(dims), "uint8"), le, re, dims)
+    cap = 64
+    count, cells, ts = ytref_trace.trace_rays(pg, np.ascontiguousarray(pos), np.ascontiguousarray(dirs),
+                                              np.ascontiguousarray(max_t), cap)
+    np.savez_compressed(HERE / "trace.npz", le=le, re=re, dims=dims, pos=pos, dirs=dirs, max_t=max_t,
+                        count=count, cells=cells, ts=ts)
+
+
+def sampler_args(p):
+    return (np.atleast_3d(p["vp_pos"]), np.atleast_3d(p["vp_dir"]), p["center"], p["bounds"], p["image"],
+            p["x_vec"], p["y_vec"], p["width"], "KDTree")
+
+
+CAMS = [((0.5, 0.5, -1.0), (1.0, 1.0, 1.0), (24, 20), "plane-parallel"),
+        ((1.3, 0.2, -0.7), (1.0, 1.0, 1.0), (24, 24), "plane-parallel"),
+        ((0.4, 0.6, -1.2), (1.5, 1.5, 1.5), (20, 24), "perspective")]
+
+
+def vr():
+    g = testing.blob_grid(16, seed=0)
+    v = np.log10(ref_vertex(g.data))
+    lg = np.log10(g.data)
+    bounds = (float(lg.min()), float(lg.max()))
+    layers = testing.ctf_layers(bounds, 4)
+    tf = glue.color_tf_from_layers(bounds, 64, layers)
+    out = {"vertex": v, "tf_y": np.array([t.y for t in tf.tables]), "tf_bounds": np.array(bounds)}
+    dims = np.array([16, 16, 16], dtype=np.int64)
+    for ci, (pos, width, res, lens) in enumerate(CAMS):
+        for ns in (1, 3):
+            cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+            p = cam.sampler_params()
+            s = RIS.VolumeRenderSampler(*sampler_args(p), tf, ns, lens_type=p["lens_type"],
+                                        camera_data=p["camera_data"], zbuffer=np.ones(res))
+            s(PartitionedGrid(0, [v], np.ones((16, 16, 16), "uint8"), np.zeros(3), np.ones(3), dims), num_threads=1)
+            out[f"img_{ci}_{ns}"] = np.array(s.aimage)
+    np.savez_compressed(HERE / "vr.npz", **out)
+
+
+def proj():
+    rng = np.random.default_rng(13)
+    cell = np.exp(rng.standard_normal((12, 12, 12)))
+    v = ref_vertex(cell)
+    dims = np.array([12, 12, 12], dtype=np.int64)
+    out = {"cell": cell}
+    for ci, (pos, width, res, lens) in enumerate(CAMS):
+        cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+        p = cam.sampler_params()
+        s = RIS.ProjectionSampler(*sampler_args(p), 1, lens_type=p["lens_type"], camera_data=p["camera_data"],
+                                  zbuffer=np.ones(res))
+        s(PartitionedGrid(0, [cell], np.ones((12, 12, 12), "uint8"), np.zeros(3), np.ones(3), dims), num_threads=1)
+        out[f"proj_{ci}"] = np.array(s.aimage)
+        cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+        p = cam.sampler_params()
+        s = RIS.InterpolatedProjectionSampler(*sampler_args(p), 2, lens_type=p["lens_type"],
+                                              camera_data=p["camera_data"], zbuffer=np.ones(res))
+        s(PartitionedGrid(0, [v], np.ones((12, 12, 12), "uint8"), np.zeros(3), np.ones(3), dims), num_threads=1)
+        out[f"iproj_{ci}"] = np.array(s.aimage)
+    np.savez_compressed(HERE / "proj.npz", **out)
+
+
+def ref_tree(gles, gres, gids, levels):
+    trunk = Node(None, None, None, np.array([-np.inf] * 3), np.array([np.inf] * 3), -1, 1)
+    for lvl in range(int(levels.max()) + 1):
+        sel = levels == lvl
+        if sel.any():
+            trunk.add_grids(int(sel.sum()), np.ascontiguousarray(gles[sel]), np.ascontiguousarray(gres[sel]),
+                            np.ascontiguousarray(gids[sel]), 0, 1)
+    return trunk
+
+
+def kd_and_amr():
+    grids = testing.amr_blob_grids(root=16, levels=2, patch=8, seed=3)
+    gles = np.array([g.left_edge for g in grids])
+    gres = np.array([g.right_edge for g in grids])
+    gids = np.array([g.id for g in grids], dtype=np.int64)
+    levels = np.array([g.level for g in grids], dtype=np.int32)
+    trunk = ref_tree(gles, gres, gids, levels)
+    leaves = list(trunk.kd_traverse())
+    le = np.array([n.get_left_edge() for n in leaves])
+    re = np.array([n.get_right_edge() for n in leaves])
+    lg = np.array([n.grid for n in leaves], dtype=np.int64)
+    vps = np.array([[0.5, 0.5, -5.0], [2.0, 0.3, 0.6], [0.2, 1.7, 1.9], [0.55, 0.45, 0.5]])
+    keyidx = {(tuple(a), tuple(b)): k for k, (a, b) in enumerate(zip(le, re))}
+    orders = []
+    for vp in vps:
+        orders.append([keyidx[(tuple(n.get_left_edge()), tuple(n.get_right_edge()))]
+                       for n in trunk.kd_traverse(viewpoint=vp)])
+    cells = [g.data for g in grids]
+    np.savez_compressed(HERE / "kd.npz", gles=gles, gres=gres, gids=gids, levels=levels, leaf_le=le, leaf_re=re,
+                        leaf_grid=lg, viewpoints=vps, orders=np.array(orders, dtype=np.int32),
+                        **{f"cell_{g.id}": g.data for g in grids})
+    # a full AMR render through the reference
+    vcd = {g.id: np.log10(ref_vertex(g.data)) for g in grids}
+    byid = {g.id: g for g in grids}
+    lg0 = np.log10(cells[0])
+    bounds = (float(lg0.min()), float(lg0.max()))
+    tf = glue.color_tf_from_layers(bounds, 128, testing.ctf_layers(bounds, 6))
+    cam = glue.Camera((0.3, 0.6, -1.1), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), (32, 28), lens_type="perspective")
+    p = cam.sampler_params()
+    s = RIS.VolumeRenderSampler(*sampler_args(p), tf, 1, lens_type=p["lens_type"], camera_data=p["camera_data"],
+                                zbuffer=np.ones((32, 28)))
+    for node in trunk.kd_traverse(viewpoint=cam.viewpoint):
+        g = byid[node.grid]
+        nle, nre = node.get_left_edge(), node.get_right_edge()
+        li = np.rint((nle - g.left_edge) / g.dds).astype("int32")
+        ri = np.rint((nre - g.left_edge) / g.dds).astype("int32")
+        dims = (ri - li).astype("int64")
+        d = vcd[g.id][li[0]: ri[0] + 1, li[1]: ri[1] + 1, li[2]: ri[2] + 1].copy()
+        s(PartitionedGrid(g.id, [d], np.ones(dims, "uint8"), nle, nre, dims), num_threads=1)
+    np.savez_compressed(HERE / "amr_vr.npz", image=np.array(s.aimage), tf_y=np.array([t.y for t in tf.tables]),
+                        tf_bounds=np.array(bounds), viewpoint=cam.viewpoint)
+
+
+if __name__ == "__main__":
+    gz()
+    trace()
+    vr()
+    proj()
+    kd_and_amr()
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)

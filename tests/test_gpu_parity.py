@@ -90,10 +90,19 @@ def test_projection_and_mip(cuda, kind, angle):
 
 
 def test_interpolated_projection_multi_sample(cuda):
-    w = workloads.uniform_vr(n=24, res=40)
+    """Projections integrate the linear (positive) field, as yt's projection
+    transfer function expects (transfer_functions.py:921-961)."""
+    from yt_gb300.amr_kdtree import AMRKDTree
+
+    kd = AMRKDTree([testing.blob_grid(24, seed=0)], log_field=False)
     cam = Camera((1.2, 0.3, -0.8), (0.5, 0.5, 0.5), (1.0, 1.0, 1.0), 40, lens_type="plane-parallel")
-    r = Renderer(w.bricks, None, device=cuda, kdtree=w.kdtree)
-    check_view(r, w.bricks, cam, _lib.INTERPOLATED_PROJECTION, n_samples=3, channels=(0,))
+    r = Renderer(kd.bricks(), None, device=cuda, kdtree=kd)
+    check_view(r, kd.bricks(), cam, _lib.INTERPOLATED_PROJECTION, n_samples=3, channels=(0,))
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=2)
+    kd = AMRKDTree(grids, log_field=False)
+    cam = Camera((0.4, 0.5, -1.0), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), 48, lens_type="perspective")
+    r = Renderer(kd.bricks(), None, device=cuda, kdtree=kd)
+    check_view(r, kd.bricks(), cam, _lib.INTERPOLATED_PROJECTION, n_samples=2, channels=(0,))
 
 
 def test_vr_multi_sample_and_zbuffer(cuda):

@@ -1,0 +1,145 @@
+"""Pin the oracle to yt's own compiled sampler through the golden fixtures
+(generated by tests/golden/make_golden.py from the reference sources).
+
+Everything here is float64 and bit-exact: the C oracle reproduces yt's
+images, traversal sequences, vertex centring and kd-tree exactly.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import cpu as ocpu
+from oracle import glue
+from yt_gb300.amr_kdtree import AMRKDTree, vertex_centred
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    return np.load(GOLD / name)
+
+
+CAMS = [((0.5, 0.5, -1.0), (1.0, 1.0, 1.0), (24, 20), "plane-parallel"),
+        ((1.3, 0.2, -0.7), (1.0, 1.0, 1.0), (24, 24), "plane-parallel"),
+        ((0.4, 0.6, -1.2), (1.5, 1.5, 1.5), (20, 24), "perspective")]
+
+
+class GoldenTF(glue.ColorTransferFunction):
+    """A ColorTransferFunction whose tables are the fixture's."""
+
+    def __init__(self, bounds, ys):
+        super().__init__(tuple(bounds), nbins=ys.shape[1])
+        for t, y in zip(self.funcs, ys):
+            t.y = y.copy()
+
+
+def test_ghost_zone_interpolate_exact():
+    f = load("gz.npz")
+    for k in ("a", "lin"):
+        assert np.array_equal(ocpu.ghost_zone_vertex_centre(f[k]), f[k + "_out"])
+        assert np.array_equal(vertex_centred(f[k]), f[k + "_out"])
+    # known answer (test_interpolators.py:107-150): a linear field is reproduced
+    i, j, k = np.meshgrid(np.arange(7), np.arange(8), np.arange(6), indexing="ij")
+    assert np.allclose(f["lin_out"], 2.0 * i - 3.0 * j + 0.5 * k + 1.0, rtol=0, atol=1e-12)
+
+
+def test_walk_volume_trace_exact():
+    f = load("trace.npz")
+    dims = f["dims"]
+    brick = ([np.zeros(tuple(dims + 1))], None, f["le"], f["re"], dims)
+    cap = f["cells"].shape[1]
+    count, cells, ts = ocpu.trace_rays(brick, f["pos"], f["dirs"], f["max_t"], cap)
+    assert np.array_equal(count, f["count"])
+    assert (f["count"] > 0).sum() > 300
+    for i in range(count.size):
+        n = min(int(count[i]), cap)
+        assert np.array_equal(cells[i, :n], f["cells"][i, :n]), i
+        assert np.array_equal(ts[i, :n].view(np.uint64), f["ts"][i, :n].view(np.uint64)), i
+
+
+@pytest.mark.parametrize("ci", range(3))
+@pytest.mark.parametrize("ns", [1, 3])
+def test_volume_render_exact(ci, ns):
+    f = load("vr.npz")
+    tf = GoldenTF(f["tf_bounds"], f["tf_y"])
+    pos, width, res, lens = CAMS[ci]
+    cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+    brick = ([f["vertex"]], None, np.zeros(3), np.ones(3), [16, 16, 16])
+    img, visits = glue.render("volume_render", cam, [brick], None, tf=tf, n_samples=ns)
+    assert visits > 0
+    assert np.array_equal(img, f[f"img_{ci}_{ns}"])
+
+
+@pytest.mark.parametrize("ci", range(3))
+def test_projections_exact(ci):
+    f = load("proj.npz")
+    cell = f["cell"]
+    pos, width, res, lens = CAMS[ci]
+    img, _ = glue.render("projection", glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens),
+                         [([cell], None, np.zeros(3), np.ones(3), [12, 12, 12])], None)
+    assert np.array_equal(img, f[f"proj_{ci}"])
+    v = ocpu.ghost_zone_vertex_centre(cell)
+    img, _ = glue.render("interpolated_projection", glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens),
+                         [([v], None, np.zeros(3), np.ones(3), [12, 12, 12])], None, n_samples=2)
+    assert np.array_equal(img, f[f"iproj_{ci}"])
+
+
+class _G:
+    def __init__(self, gid, level, le, re, data):
+        self.id, self.level, self.left_edge, self.right_edge, self.data = gid, level, le, re, data
+        self.dims = np.array(data.shape, dtype=np.int64)
+
+    @property
+    def dds(self):
+        return (self.right_edge - self.left_edge) / self.dims
+
+
+def golden_grids():
+    f = load("kd.npz")
+    return f, [_G(int(i), int(l), a, b, f[f"cell_{int(i)}"])
+               for i, l, a, b in zip(f["gids"], f["levels"], f["gles"], f["gres"])]
+
+
+def test_kdtree_oracle_and_product_exact():
+    f, grids = golden_grids()
+    ot = glue.KDTree(grids)
+    leaves = ot.leaves()
+    assert len(leaves) == f["leaf_le"].shape[0]
+    for k, n in enumerate(leaves):
+        assert np.array_equal(n.le, f["leaf_le"][k]) and np.array_equal(n.re, f["leaf_re"][k])
+        assert n.grid == f["leaf_grid"][k]
+    kd = AMRKDTree(grids)
+    assert np.array_equal(kd.leaf_le, f["leaf_le"]) and np.array_equal(kd.leaf_re, f["leaf_re"])
+    assert np.array_equal(kd.leaf_grid, f["leaf_grid"])
+    idx = {id(n): k for k, n in enumerate(leaves)}
+    for vp, want in zip(f["viewpoints"], f["orders"]):
+        assert [idx[id(n)] for n in ot.leaves(vp)] == list(want)
+        assert np.array_equal(kd.viewpoint_order(vp), want)
+
+
+def test_kd_leaves_tile_the_domain():
+    """kd_sum_volume (amr_kdtools.pyx:534-543): leaves with a grid tile the
+    root grid's domain."""
+    f, grids = golden_grids()
+    vol = np.prod(f["leaf_re"] - f["leaf_le"], axis=1).sum()
+    assert abs(vol - 1.0) < 1e-12
+
+
+def test_amr_volume_render_exact():
+    f, grids = golden_grids()
+    g = load("amr_vr.npz")
+    tf = GoldenTF(g["tf_bounds"], g["tf_y"])
+    ot = glue.KDTree(grids)
+    byid = {gr.id: gr for gr in grids}
+    vcd = {}
+    cam = glue.Camera((0.3, 0.6, -1.1), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), (32, 28), lens_type="perspective")
+    assert np.array_equal(cam.viewpoint, g["viewpoint"])
+    bricks = []
+    for node in ot.leaves(cam.viewpoint):
+        gr = byid[node.grid]
+        if gr.id not in vcd:
+            vcd[gr.id] = [glue.vertex_centred(gr.data, True)]
+        bricks.append(glue.brick_data(node, gr, vcd[gr.id]))
+    img, _ = glue.render("volume_render", cam, bricks, None, tf=tf)
+    assert np.array_equal(img, g["image"])

@@ -131,7 +131,7 @@ def lognormal_grf(n=512, seed=1, slope=-3.0, dtype=np.float32) -> np.ndarray:
     nz = k > 0
     amp[nz] = k[nz] ** (slope / 2.0)
     fk *= amp
-    g = np.fft.irfftn(fk, s=(n, n, n))
+    g = np.fft.irfftn(fk, s=(n, n, n), axes=(0, 1, 2))
     g -= g.mean()
     g /= g.std()
     return np.exp(g).astype(dtype)
