@@ -287,6 +287,8 @@ def run_ours(args):
     samples_total = int(r.counters[0].item())
     rays = int(r.counters[2].item()) // max(args.steps, 1)
     samples_step = samples_total // args.steps
+    walks_step = int(r.counters[1].item()) // max(args.steps, 1)
+    guarded_step = int(r.counters[3].item()) // max(args.steps, 1)
     t_total = float(ms.sum()) / 1e3
     if world > 1:
         import torch.distributed as dist
@@ -337,7 +339,8 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32 sampling / f64 traversal", "data": "synthetic",
             "config": config_dict(w, args),
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
-            "samples_per_step": samples_step, "rays_per_step": rays,
+            "samples_per_step": samples_step, "rays_per_step": rays, "brick_walks_per_step": walks_step,
+            "out_of_brick_cells_per_step": guarded_step,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
                          "peak_source": peak_kind + " hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"

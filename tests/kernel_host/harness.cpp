@@ -1,0 +1,62 @@
+// CPU build of the sampler kernels' per-ray walk -- TEST INFRASTRUCTURE.
+//
+// Compiles yt_gb300/csrc/ytgb_ray.cuh (the exact source the GPU kernels
+// run per ray) with g++ and -ffp-contract=off and drives it over every pixel
+// and brick the way render_kernel does (without the block binning), so
+// tests can check the walk, geometry and compositing logic against the
+// oracle on machines without a GPU.  The product never loads this library.
+#include <vector>
+#include "ytgb.h"
+#include "ytgb_ray.cuh"
+using namespace ytgb;
+
+template <int MODE, int CTF>
+static void run(const ytgb_render_args &a, unsigned long long *hashes, long long *counts, unsigned long long *cnt) {
+    std::vector<float4> tab;
+    if (MODE == MODE_VR) {
+        const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
+        int nb = a.tf.nbins_max;
+        if (CTF) {
+            tab.resize(3 * nb);
+            for (int b = 0; b < nb; b++) {
+                float4 t0 = g[b], t1 = g[nb + b], t2 = g[2 * nb + b], t3 = g[3 * nb + b];
+                tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
+                tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
+                tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
+            }
+        } else {
+            tab.assign(g, g + a.tf.n_fits * nb);
+        }
+    }
+    const int4 *rects = reinterpret_cast<const int4 *>(a.rects);
+    for (int vi = 0; vi < a.view.nx; vi++)
+        for (int vj = 0; vj < a.view.ny; vj++) {
+            size_t p = (size_t)vi * a.view.ny + vj;
+            Ray r;
+            make_ray(a.view, vi, vj, r);
+            double *img = a.image ? a.image + p * 4 : nullptr;
+            RayState st;
+            ray_state_init(st, MODE != MODE_TRACE ? img : nullptr, a.zbuffer ? a.zbuffer[p] : 1.0, a.zbuffer != nullptr, a.flags);
+            if (MODE == MODE_TRACE) { st.th = hashes[p]; st.tcount = counts[p]; }
+            for (int k = 0; k < a.n_order; k++) {
+                int4 rc = rects[k];
+                if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
+                walk_brick<MODE, CTF>(a, tab.data(), r, a.order[k], st);
+            }
+            if (MODE == MODE_TRACE) { hashes[p] = st.th; counts[p] = st.tcount; }
+            else for (int c = 0; c < 4; c++) if (st.touched & (1u << c)) img[c] = (double)st.xh[c] + (double)st.xl[c];
+            cnt[0] += st.visits; cnt[1] += st.walks; cnt[3] += st.guarded; cnt[2]++;
+        }
+}
+
+extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long long *hashes, long long *counts,
+                          unsigned long long *cnt) {
+    if (trace) { run<MODE_TRACE, 0>(*a, hashes, counts, cnt); return 0; }
+    switch (a->kind) {
+    case YTGB_VOLUME_RENDER: if (a->tf.ctf_fast) run<MODE_VR, 1>(*a, 0, 0, cnt); else run<MODE_VR, 0>(*a, 0, 0, cnt); break;
+    case YTGB_PROJECTION: run<MODE_PROJ, 0>(*a, 0, 0, cnt); break;
+    case YTGB_INTERPOLATED_PROJECTION: run<MODE_IPROJ, 0>(*a, 0, 0, cnt); break;
+    default: run<MODE_MIP, 0>(*a, 0, 0, cnt);
+    }
+    return 0;
+}

@@ -130,14 +130,18 @@ def test_grey_opacity_and_weighted_tables(cuda):
     cam = Camera((1.1, 0.4, -0.9), (0.5, 0.5, 0.5), (1.0, 1.0, 1.0), 48, lens_type="plane-parallel")
     r = Renderer(bricks, ctf, device=cuda)
     check_view(r, bricks, cam, _lib.VOLUME_RENDER, tf=ctf, channels=(0, 1, 2, 3))
-    # multivariate TF: emission from field 1 weighted by field 0's table
+    # multivariate TF
     mv = MultiVariateTransferFunction()
     t0 = TransferFunction((lo, hi), 64)
     t0.add_gaussian(0.5 * (lo + hi), 0.05, 1.0)
-    t1 = TransferFunction((float(v1.min()) - 0.1, float(v1.max()) + 0.1), 200)
-    t1.add_gaussian(float(v1.mean()), 0.3, 0.8)
+    # a second table on field 0 weighted by the positive linear field 1 and
+    # by table 0 (emission from one table, weighted by density and another
+    # table).  Weighting by a signed field instead would amplify the float32
+    # storage error of the data near its zero crossings.
+    t1 = TransferFunction((lo, hi), 200)
+    t1.add_gaussian(0.7 * lo + 0.3 * hi, 0.05, 0.8)
     mv.add_field_table(t0, 0)
-    mv.add_field_table(t1, 1, weight_field_id=0, weight_table_id=0)
+    mv.add_field_table(t1, 0, weight_field_id=1, weight_table_id=0)
     mv.link_channels(1, [0, 1, 2])
     r2 = Renderer(bricks, mv, device=cuda)
     check_view(r2, bricks, cam, _lib.VOLUME_RENDER, tf=mv)

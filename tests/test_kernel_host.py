@@ -1,0 +1,181 @@
+"""The GPU kernels' per-ray walk, compiled for the CPU, against the oracle.
+
+tests/kernel_host/harness.cpp builds yt_gb300/csrc/ytgb_ray.cuh -- the same
+source render_kernel executes per ray -- with g++ (no floating-point
+contraction), so these cases check the exact traversal (trace hashes), the
+float32 sample geometry and the compensated compositing without a GPU.  The
+bar is the GPU parity bar: bit-identical traces and visit counts, image
+within 1e-5 per-pixel relative error.
+"""
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import cpu as ocpu
+from yt_gb300 import _lib, testing, workloads
+from yt_gb300.amr_kdtree import AMRKDTree, vertex_centred
+from yt_gb300.camera import Camera
+from yt_gb300.image_samplers import make_view
+from yt_gb300.render import relative_error
+from yt_gb300.transfer_functions import (ColorTransferFunction, MultiVariateTransferFunction, TransferFunction,
+                                         pack)
+from yt_gb300.volume import BrickSet
+
+ROOT = Path(__file__).resolve().parent.parent
+HERE = Path(__file__).resolve().parent / "kernel_host"
+KN = {0: "volume_render", 1: "projection", 2: "interpolated_projection", 3: "mip"}
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def emu():
+    src = HERE / "harness.cpp"
+    out = HERE / "_build" / "libytgb_host_walk.so"
+    deps = [src, ROOT / "yt_gb300" / "csrc" / "ytgb_ray.cuh", ROOT / "include" / "ytgb.h",
+            ROOT / "yt_gb300" / "csrc" / "ytgb_internal.h"]
+    if not out.exists() or out.stat().st_mtime < max(d.stat().st_mtime for d in deps):
+        out.parent.mkdir(exist_ok=True)
+        tmp = out.with_suffix(f".{os.getpid()}.tmp")
+        cuda_inc = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/include"
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                        f"-I{ROOT / 'include'}", f"-I{ROOT / 'yt_gb300' / 'csrc'}", f"-I{cuda_inc}", str(src),
+                        "-o", str(tmp)], check=True)
+        os.replace(tmp, out)
+    L = C.CDLL(str(out))
+    L.emu_render.argtypes = [C.POINTER(_lib.RenderArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    return L
+
+
+def run_emu(L, bricks, cam, order, kind, tf=None, ns=1, zbuffer=None):
+    bs = BrickSet(bricks, device="cpu")
+    p = cam.sampler_params()
+    nx, ny = cam.resolution
+    view, ppos, pdir = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
+                                 p["y_vec"], p["width"], p["lens_type"], p["camera_data"])
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    rects = np.ascontiguousarray(bs.rects(view, order))
+    a = _lib.RenderArgs()
+    a.kind, a.n_samples, a.n_order, a.view = kind, ns, order.size, view
+    if ppos is not None:
+        a.view.px_pos, a.view.px_dir = ppos.ctypes.data, pdir.ctypes.data
+    a.bricks, a.order, a.rects, a.data = bs.desc.data_ptr(), order.ctypes.data, rects.ctypes.data, bs.data.data_ptr()
+    keep = []
+    if bs.masks is not None:
+        a.masks = bs.masks.data_ptr()
+    if tf is not None:
+        pk = pack(tf)
+        keep.append(pk)
+        a.tf, a.tf_tables = pk.header, pk.tables.ctypes.data
+    if zbuffer is not None:
+        zbuffer = np.ascontiguousarray(zbuffer, dtype=np.float64)
+        a.zbuffer = zbuffer.ctypes.data
+    img = np.zeros((nx, ny, 4))
+    a.image = img.ctypes.data
+    cnt = np.zeros(4, dtype=np.uint64)
+    L.emu_render(C.byref(a), 0, None, None, cnt.ctypes.data)
+    h = np.full(nx * ny, _lib.FNV_OFFSET, dtype=np.uint64)
+    c = np.zeros(nx * ny, dtype=np.int64)
+    L.emu_render(C.byref(a), 1, h.ctypes.data, c.ctypes.data, np.zeros(4, dtype=np.uint64).ctypes.data)
+    return img, cnt, h.reshape(nx, ny), c.reshape(nx, ny)
+
+
+def run_oracle(bricks, cam, order, kind, tf=None, ns=1, zbuffer=None):
+    p = cam.sampler_params()
+    s = ocpu.OracleSampler(KN[kind], p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"], p["x_vec"],
+                           p["y_vec"], p["width"], lens_type=p["lens_type"], camera_data=p["camera_data"],
+                           zbuffer=zbuffer, n_samples=ns, tf=tf)
+    ob = ocpu.OracleBricks(bricks)
+    visits = s.render(ob, order)
+    h, c = s.trace(ob, order)
+    return p["image"], visits, h, c
+
+
+def check(L, bricks, cam, order, kind, tf=None, ns=1, channels=(0, 1, 2), zbuffer=None):
+    img, cnt, h, c = run_emu(L, bricks, cam, order, kind, tf, ns, zbuffer)
+    ref, visits, hr, cr = run_oracle(bricks, cam, order, kind, tf, ns, zbuffer)
+    mx, rms = relative_error(img, ref, channels=channels)
+    assert mx <= TOL, f"max relative error {mx:.3e} (rms {rms:.3e})"
+    assert int(cnt[0]) == visits
+    if zbuffer is None:
+        assert np.array_equal(c, cr) and np.array_equal(h, hr)
+    return mx
+
+
+@pytest.mark.parametrize("pos,lens,width", [((0.5, 0.5, -1.0), "plane-parallel", 1.0),
+                                            ((1.3, 0.2, -0.7), "plane-parallel", 1.0),
+                                            ((-0.4, 1.1, 1.6), "plane-parallel", 0.8),
+                                            ((1.6, 1.4, 1.9), "perspective", 1.5),
+                                            ((0.45, 0.55, 0.5), "perspective", 1.5)])
+def test_uniform_vr(emu, pos, lens, width):
+    w = workloads.uniform_vr(n=24, res=40)
+    cam = Camera(pos, (0.5, 0.5, 0.5), width, (40, 36), lens_type=lens)
+    check(emu, w.bricks, cam, w.order(cam), _lib.VOLUME_RENDER, tf=w.tf)
+
+
+@pytest.mark.parametrize("lens", ["perspective", "plane-parallel"])
+def test_amr_vr(emu, lens):
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=64, lens_type=lens)
+    cam = w.views[0].camera if lens == "perspective" else Camera((1.4, -0.3, 1.2), (0.5, 0.5, 0.5), 1.2, 64)
+    check(emu, w.bricks, cam, w.order(cam), _lib.VOLUME_RENDER, tf=w.tf)
+
+
+@pytest.mark.parametrize("kind", [_lib.PROJECTION, _lib.MIP])
+@pytest.mark.parametrize("angle", [0.0, 30.0, 57.0])
+def test_projection_mip(emu, kind, angle):
+    w = workloads.projection_study(n=24, res=40, angles=(angle,), kinds=(kind,))
+    check(emu, w.bricks, w.views[0].camera, np.array([0]), kind, channels=(0,))
+
+
+def test_interpolated_projection(emu):
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=2)
+    kd = AMRKDTree(grids, log_field=False)
+    for cam, ns in ((Camera((0.4, 0.5, -1.0), 0.5, 1.5, 40, lens_type="perspective"), 2),
+                    (Camera((1.2, 0.3, -0.8), 0.5, 1.0, 40), 3)):
+        check(emu, kd.bricks(), cam, kd.viewpoint_order(cam.viewpoint), _lib.INTERPOLATED_PROJECTION, ns=ns,
+              channels=(0,))
+
+
+def test_zbuffer_and_samples(emu):
+    w = workloads.uniform_vr(n=20, res=32)
+    cam = Camera((0.2, 1.3, -0.8), 0.5, 1.0, 32)
+    zb = np.random.default_rng(3).uniform(0.2, 1.5, (32, 32))
+    check(emu, w.bricks, cam, w.order(cam), _lib.VOLUME_RENDER, tf=w.tf, ns=4, zbuffer=zb)
+
+
+def test_grey_opacity_and_multivariate(emu):
+    g = testing.blob_grid(20, seed=5)
+    v0 = np.log10(vertex_centred(g.data))
+    v1 = vertex_centred(np.sqrt(g.data))
+    bricks = [([v0, v1], None, np.zeros(3), np.ones(3), np.array([20, 20, 20]))]
+    lo, hi = float(np.nanmin(v0)), float(np.nanmax(v0))
+    ctf = ColorTransferFunction((lo, hi), nbins=128, grey_opacity=True)
+    for loc, wd, rgba in testing.ctf_layers((lo, hi), 3, width=0.02):
+        ctf.add_gaussian(loc, wd, list(rgba))
+    cam = Camera((1.1, 0.4, -0.9), 0.5, 1.0, 40)
+    check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=ctf, channels=(0, 1, 2, 3))
+    mv = MultiVariateTransferFunction()
+    t0 = TransferFunction((lo, hi), 64)
+    t0.add_gaussian(0.5 * (lo + hi), 0.05, 1.0)
+    # a second table on field 0 weighted by the positive linear field 1 and
+    # by table 0 (emission from one table, weighted by density and another
+    # table).  Weighting by a signed field instead would amplify the float32
+    # storage error of the data near its zero crossings.
+    t1 = TransferFunction((lo, hi), 200)
+    t1.add_gaussian(0.7 * lo + 0.3 * hi, 0.05, 0.8)
+    mv.add_field_table(t0, 0)
+    mv.add_field_table(t1, 0, weight_field_id=1, weight_table_id=0)
+    mv.link_channels(1, [0, 1, 2])
+    check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=mv)
+
+
+def test_masked_cells(emu):
+    w = workloads.uniform_vr(n=16, res=32)
+    data, _, le, re, dims = w.bricks[0]
+    mask = (np.random.default_rng(7).random(tuple(dims)) < 0.7).astype(np.uint8)
+    bricks = [(data, mask, le, re, dims)]
+    cam = Camera((1.2, 0.3, -0.8), 0.5, 1.0, 32)
+    check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=w.tf)
