@@ -33,10 +33,13 @@ extern "C" {
 #define YTGB_INTERPOLATED_PROJECTION 2
 #define YTGB_MIP 3
 
-/* ray generation: generate_vector_info_plane_parallel (lenses.pyx:179-192)
- * or generate_vector_info_null, i.e. per-pixel arrays (lenses.pyx:196-207) */
+/* ray generation: generate_vector_info_plane_parallel (lenses.pyx:179-192);
+ * generate_vector_info_null, i.e. per-pixel arrays (lenses.pyx:196-207); or
+ * the per-pixel rays of PerspectiveLens._get_sampler_params (lens.py:166-234)
+ * computed on the device from the camera instead of read from arrays */
 #define YTGB_LENS_PLANE_PARALLEL 0
 #define YTGB_LENS_PER_PIXEL 1
+#define YTGB_LENS_PERSPECTIVE 2
 
 /* pixel culling: calculate_extent_plane_parallel / _perspective / _null
  * (lenses.pyx:22-55, :60-161, :169-175) */
@@ -46,6 +49,7 @@ extern "C" {
 
 /* render flags */
 #define YTGB_FLAG_NO_COMPENSATION 1u   /* plain FP32 accumulation (precision study) */
+#define YTGB_FLAG_TILE_SHIFT 8         /* bits 8..11: tile shape 0 = 8x16, 1 = 16x8, 2 = 4x32 pixels */
 
 /* One brick: the fields of yt's VolumeContainer (volume_container.pxd:13-33,
  * filled by PartitionedGrid.__cinit__, partitioned_grid.pyx:28-63).  The
@@ -71,8 +75,9 @@ typedef struct ytgb_view {
     int32_t nx, ny;           /* image.shape[0], image.shape[1] (nv) */
     int32_t lens;             /* YTGB_LENS_* */
     int32_t extent;           /* YTGB_EXTENT_* */
-    double vp_pos[12];        /* plane-parallel: inv_mat.ravel('F') + back_center */
-    double vp_dir[3];         /* plane-parallel: normal * width[2] */
+    double vp_pos[12];        /* plane-parallel: inv_mat.ravel('F') + back_center;
+                               * perspective: position, east, north, normal */
+    double vp_dir[3];         /* plane-parallel: normal * width[2]; perspective: width */
     double center[3];
     double bounds[4];
     double x_vec[3];
@@ -80,6 +85,7 @@ typedef struct ytgb_view {
     double width[3];
     double camera_data[15];   /* position, width, east, north, normal */
     double pdx, pdy;          /* (bounds[1]-bounds[0])/nx, (bounds[3]-bounds[2])/ny */
+    double ray_scale;         /* perspective: max_length / width[2] (lens.py:204-211) */
     const double *px_pos;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
     const double *px_dir;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
 } ytgb_view;
@@ -129,6 +135,17 @@ typedef struct ytgb_render_args {
     int32_t *error;            /* device error word (0 = ok), or NULL */
 } ytgb_render_args;
 
+/* One view of a multi-view batch (device memory), as filled by
+ * ytgb_batch_plan: the view's render arguments plus its place in the batch's
+ * tile numbering. */
+typedef struct ytgb_batch_entry {
+    ytgb_render_args args;
+    int32_t tile_begin;  /* first work item of this view */
+    int32_t tiles_y;     /* tiles along the image's second axis */
+    int32_t tiles;       /* work items of this view */
+    int32_t pad;
+} ytgb_batch_entry;
+
 /* ---- status -------------------------------------------------------------- */
 int ytgb_abi_version(void);
 const char *ytgb_last_error(void);
@@ -165,6 +182,22 @@ int ytgb_render(const ytgb_render_args *args, void *stream);
  * 26-140) hands to the sampler, and the visit count.  hashes/counts are
  * device (nx*ny) arrays, initialised by the caller (FNV offset basis, 0). */
 int ytgb_trace(const ytgb_render_args *args, unsigned long long *hashes, long long *counts, void *stream);
+
+/* ---- device: many views in one persistent launch ------------------------- */
+/* Host: validate a batch (host copy of the entries; all of one sampler kind
+ * and table layout) and number its tiles for a tile shape.  Writes
+ * tile_begin / tiles_y / tiles of each entry, the total work items and the
+ * shared memory the launch needs.  The same render as calling ytgb_render
+ * for every entry; there is no reference counterpart (yt renders one
+ * camera at a time). */
+int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t tile_shape, int32_t *total_tiles,
+                    int32_t *smem_bytes);
+/* Device: render a planned batch (entries copied to device memory) with one
+ * persistent launch of `blocks` blocks (<= 0: one wave of the GPU) pulling
+ * work items from *d_queue, which it resets first.  Graph-capturable. */
+int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+                      int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
+                      int32_t blocks, void *stream);
 
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over

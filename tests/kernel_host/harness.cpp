@@ -60,3 +60,17 @@ extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long lo
     }
     return 0;
 }
+
+// the rays make_ray generates for every pixel (positions and directions)
+extern "C" void emu_rays(const ytgb_view *v, double *pos, double *dir) {
+    for (int vi = 0; vi < v->nx; vi++)
+        for (int vj = 0; vj < v->ny; vj++) {
+            Ray r;
+            make_ray(*v, vi, vj, r);
+            size_t o = ((size_t)vi * v->ny + vj) * 3;
+            for (int i = 0; i < 3; i++) {
+                pos[o + i] = r.pos[i];
+                dir[o + i] = r.dir[i];
+            }
+        }
+}

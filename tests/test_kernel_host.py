@@ -47,6 +47,7 @@ def emu():
         os.replace(tmp, out)
     L = C.CDLL(str(out))
     L.emu_render.argtypes = [C.POINTER(_lib.RenderArgs), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.emu_rays.argtypes = [C.POINTER(_lib.View), C.c_void_p, C.c_void_p]
     return L
 
 
@@ -179,3 +180,43 @@ def test_masked_cells(emu):
     bricks = [(data, mask, le, re, dims)]
     cam = Camera((1.2, 0.3, -0.8), 0.5, 1.0, 32)
     check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=w.tf)
+
+
+@pytest.mark.parametrize("pos,res", [((0.5, 0.5, -1.0), (64, 64)), ((1.6, 1.4, 1.9), (48, 40)),
+                                     ((0.1, 0.9, 0.3), (1, 7)), ((-2.0, 0.3, 0.2), (33, 1))])
+def test_device_perspective_rays_match_numpy(emu, pos, res):
+    """YTGB_LENS_PERSPECTIVE regenerates PerspectiveLens's numpy rays
+    (lens.py:186-225) bit for bit."""
+    cam = Camera(pos, (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), res, lens_type="perspective")
+    p = cam.sampler_params()
+    v = Camera(pos, (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), res, lens_type="perspective").device_view()
+    nx, ny = res
+    got_p = np.zeros((nx, ny, 3))
+    got_d = np.zeros((nx, ny, 3))
+    emu.emu_rays(C.byref(v), got_p.ctypes.data, got_d.ctypes.data)
+    assert np.array_equal(got_p, p["vp_pos"])
+    assert np.array_equal(got_d, p["vp_dir"])
+    # the view's culling parameters equal the per-pixel sampler's
+    view, _, _ = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"], p["y_vec"],
+                           p["width"], p["lens_type"], p["camera_data"])
+    assert list(view.camera_data) == list(v.camera_data) and view.extent == v.extent
+    assert list(view.center) == list(v.center) and view.pdx == v.pdx and view.pdy == v.pdy
+
+
+def test_device_perspective_render_matches_oracle(emu):
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=48)
+    cam = w.views[0].camera
+    bs = BrickSet(w.bricks, device="cpu")
+    order = np.ascontiguousarray(w.order(cam), dtype=np.int32)
+    view = cam.device_view()
+    rects = np.ascontiguousarray(bs.rects(view, order))
+    a = _lib.RenderArgs()
+    a.kind, a.n_samples, a.n_order, a.view = _lib.VOLUME_RENDER, 1, order.size, view
+    a.bricks, a.order, a.rects, a.data = bs.desc.data_ptr(), order.ctypes.data, rects.ctypes.data, bs.data.data_ptr()
+    pk = pack(w.tf)
+    a.tf, a.tf_tables = pk.header, pk.tables.ctypes.data
+    img = np.zeros((48, 48, 4))
+    a.image = img.ctypes.data
+    emu.emu_render(C.byref(a), 0, None, None, np.zeros(4, dtype=np.uint64).ctypes.data)
+    ref, *_ = run_oracle(w.bricks, cam, order, _lib.VOLUME_RENDER, w.tf)
+    assert relative_error(img, ref)[0] <= TOL

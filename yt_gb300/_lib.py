@@ -15,9 +15,10 @@ LIB_PATH = Path(__file__).resolve().parent / "lib" / "libytgb.so"
 
 OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE = 0, -1, -2, -3
 VOLUME_RENDER, PROJECTION, INTERPOLATED_PROJECTION, MIP = 0, 1, 2, 3
-LENS_PLANE_PARALLEL, LENS_PER_PIXEL = 0, 1
+LENS_PLANE_PARALLEL, LENS_PER_PIXEL, LENS_PERSPECTIVE = 0, 1, 2
 EXTENT_PLANE_PARALLEL, EXTENT_PERSPECTIVE, EXTENT_NULL = 0, 1, 2
 FLAG_NO_COMPENSATION = 1
+FLAG_TILE_SHIFT = 8
 FNV_OFFSET = 1469598103934665603
 
 _dp = C.POINTER(C.c_double)
@@ -54,6 +55,7 @@ class View(C.Structure):
         ("camera_data", C.c_double * 15),
         ("pdx", C.c_double),
         ("pdy", C.c_double),
+        ("ray_scale", C.c_double),
         ("px_pos", C.c_void_p),
         ("px_dir", C.c_void_p),
     ]
@@ -98,6 +100,16 @@ class RenderArgs(C.Structure):
     ]
 
 
+class BatchEntry(C.Structure):
+    _fields_ = [
+        ("args", RenderArgs),
+        ("tile_begin", C.c_int32),
+        ("tiles_y", C.c_int32),
+        ("tiles", C.c_int32),
+        ("pad", C.c_int32),
+    ]
+
+
 class YtgbError(RuntimeError):
     pass
 
@@ -117,6 +129,10 @@ SIGNATURES = {
                                C.POINTER(TF), C.c_void_p]),
     "ytgb_render": (C.c_int, [C.POINTER(RenderArgs), C.c_void_p]),
     "ytgb_trace": (C.c_int, [C.POINTER(RenderArgs), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_batch_plan": (C.c_int, [C.POINTER(BatchEntry), C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32)]),
+    "ytgb_batch_render": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_void_p, C.c_int32, C.c_void_p]),
     "ytgb_kdtree_build": (C.c_void_p, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_kdtree_destroy": (None, [C.c_void_p]),
     "ytgb_kdtree_num_leaves": (C.c_int32, [C.c_void_p]),

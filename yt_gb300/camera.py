@@ -17,6 +17,8 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import _lib
+
 
 def orientation(normal_vector, north_vector=None):
     """Return (unit_vectors [east, north, normal], inv_mat)."""
@@ -125,3 +127,48 @@ class Camera:
             "image": np.zeros((nx, ny, 4), dtype="float64"),
             "lens_type": "perspective",
         }
+
+    def device_view(self):
+        """The ``ytgb_view`` of this camera with rays generated on the device.
+
+        Plane-parallel views carry yt's 12 + 3 ray parameters.  Perspective
+        views carry the camera instead of yt's (nx, ny, 3) ray arrays
+        (``YTGB_LENS_PERSPECTIVE``): position, the unit vectors, the width
+        (with width[1] = width[0] * ny / nx as ``lens.py:176-178`` sets it)
+        and max_length / width[2]; the kernel recomputes yt's per-pixel
+        vectors (``lens.py:186-225``) bit for bit."""
+        if self.lens_type == "plane-parallel":
+            from .image_samplers import make_view
+
+            p = self.sampler_params()
+            nx, ny = self.resolution
+            v, _, _ = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
+                                p["y_vec"], p["width"], p["lens_type"], p["camera_data"])
+            return v
+        nx, ny = self.resolution
+        self.width[1] = self.width[0] * (ny / nx)
+        uv = self.unit_vectors
+        v = _lib.View()
+        v.nx, v.ny = nx, ny
+        v.lens = _lib.LENS_PERSPECTIVE
+        v.extent = _lib.EXTENT_PERSPECTIVE
+        for i in range(3):
+            v.vp_pos[i] = float(self.position[i])
+            v.vp_pos[3 + i] = float(uv[0][i])
+            v.vp_pos[6 + i] = float(uv[1][i])
+            v.vp_pos[9 + i] = float(uv[2][i])
+            v.vp_dir[i] = float(self.width[i])
+            v.center[i] = float(self.back_center[i])
+            v.x_vec[i] = 1.0
+            v.y_vec[i] = 1.0
+            v.width[i] = float(self.width[i])
+        for i, b in enumerate((0.0, 1.0, 0.0, 1.0)):
+            v.bounds[i] = b
+        v.pdx = (v.bounds[1] - v.bounds[0]) / nx
+        v.pdy = (v.bounds[3] - v.bounds[2]) / ny
+        max_length = np.linalg.norm(self.position - self.domain_center) + 0.5 * np.linalg.norm(self.domain_width)
+        v.ray_scale = float(max_length / self.width[2])
+        cd = np.vstack((self.position, self.width, uv)).ravel()
+        for i in range(15):
+            v.camera_data[i] = float(cd[i])
+        return v

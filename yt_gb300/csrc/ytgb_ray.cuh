@@ -100,6 +100,23 @@ YTGB_HD void make_ray(const ytgb_view &v, int vi, int vj, Ray &r) {
         r.pos[2] = dadd(dadd(dmul(v.vp_pos[2], px), dmul(v.vp_pos[5], py)), v.vp_pos[11]);
         YTGB_UNROLL
         for (int i = 0; i < 3; i++) r.dir[i] = v.vp_dir[i];
+    } else if (v.lens == YTGB_LENS_PERSPECTIVE) {
+        // PerspectiveLens._get_sampler_params (lens.py:186-225) for one pixel:
+        // px = linspace(-0.5, 0.5, nx)[vi] (numpy: i*step + start, last = stop),
+        // vector = (w0*(east*px) + w1*(north*py) + normal*w2) * (max_length/w2)
+        const double px = (v.nx > 1 && vi == v.nx - 1)
+                              ? 0.5
+                              : dadd(dmul((double)vi, v.nx > 1 ? ddiv(1.0, (double)(v.nx - 1)) : 0.0), -0.5);
+        const double py = (v.ny > 1 && vj == v.ny - 1)
+                              ? 0.5
+                              : dadd(dmul((double)vj, v.ny > 1 ? ddiv(1.0, (double)(v.ny - 1)) : 0.0), -0.5);
+        YTGB_UNROLL
+        for (int i = 0; i < 3; i++) {
+            const double sx = dmul(v.vp_dir[0], dmul(v.vp_pos[3 + i], px));
+            const double sy = dmul(v.vp_dir[1], dmul(v.vp_pos[6 + i], py));
+            r.dir[i] = dmul(dadd(dadd(sx, sy), dmul(v.vp_pos[9 + i], v.vp_dir[2])), v.ray_scale);
+            r.pos[i] = v.vp_pos[i];
+        }
     } else {
         size_t o = ((size_t)vi * v.ny + vj) * 3;
         YTGB_UNROLL

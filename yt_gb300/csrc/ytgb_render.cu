@@ -51,46 +51,69 @@ namespace {
 
 using namespace ytgb;
 
-constexpr int TILE_X = 8;    // image rows (vi) per block
-constexpr int TILE_Y = 16;   // image columns (vj) per block
-constexpr int BLOCK = TILE_X * TILE_Y;
+// Tile shapes (image rows vi x image columns vj per block); the autotuner
+// picks one per workload class.  All shapes are 128 threads.
+template <int TS> struct TileShape;
+template <> struct TileShape<0> { static constexpr int X = 8, Y = 16; };
+template <> struct TileShape<1> { static constexpr int X = 16, Y = 8; };
+template <> struct TileShape<2> { static constexpr int X = 4, Y = 32; };
+constexpr int BLOCK = 128;
 constexpr int NWARP = BLOCK / 32;
 
-// CTF = 1: ColorTransferFunction layout -- one bin lookup serves all four
-// tables, packed per bin in shared memory as y[4], dy[4] and the d0 pair.
-template <int MODE, int CTF>
-__global__ void __launch_bounds__(BLOCK) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
-                                                       long long *counts) {
-    extern __shared__ float4 s_tab[];
-    __shared__ unsigned long long s_cnt[4];
-    __shared__ int s_sel[BLOCK];
-    __shared__ int s_wsum[NWARP];
+struct TileSmem {
+    unsigned long long cnt[4];
+    int sel[BLOCK];
+    int wsum[NWARP];
+    const float *tab_src;  // tables currently staged in s_tab
+    int tab_ctf;
+    int item;
+};
+
+// One tile of one view: cast_through_kdtree (image_samplers.pyx:146-197) for
+// every brick of the view, restricted to this tile's pixels.  The ordered
+// brick list is binned against the tile by the bricks' pixel rectangles
+// (ballot + prefix in shared memory, BLOCK bricks per pass, order kept); each
+// ray then walks the selected bricks whose rectangle holds its pixel.
+template <int MODE, int CTF, int TS>
+__device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, int by, float4 *s_tab, TileSmem &sm,
+                                            unsigned long long *hashes, long long *counts) {
+    constexpr int TX = TileShape<TS>::X, TY = TileShape<TS>::Y;
     const ytgb_view &v = a.view;
     const int tid = threadIdx.x;
-    if (tid < 4) s_cnt[tid] = 0;
+    if (tid < 4) sm.cnt[tid] = 0;
     if (MODE == MODE_VR) {
-        const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
-        if (CTF) {
+        // stage the transfer function unless this block already holds it
+        const float *src = a.tf_tables;
+        const bool reload = sm.tab_src != src || sm.tab_ctf != CTF;
+        if (reload) {
+            const float4 *g = reinterpret_cast<const float4 *>(src);
             const int nb = a.tf.nbins_max;
-            for (int b = tid; b < nb; b += BLOCK) {
-                float4 t0 = __ldg(g + 0 * nb + b), t1 = __ldg(g + 1 * nb + b);
-                float4 t2 = __ldg(g + 2 * nb + b), t3 = __ldg(g + 3 * nb + b);
-                s_tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
-                s_tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
-                s_tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
+            if (CTF) {
+                for (int b = tid; b < nb; b += BLOCK) {
+                    float4 t0 = __ldg(g + 0 * nb + b), t1 = __ldg(g + 1 * nb + b);
+                    float4 t2 = __ldg(g + 2 * nb + b), t3 = __ldg(g + 3 * nb + b);
+                    s_tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
+                    s_tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
+                    s_tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
+                }
+            } else {
+                const int n = a.tf.n_fits * nb;
+                for (int k = tid; k < n; k += BLOCK) s_tab[k] = __ldg(g + k);
             }
-        } else {
-            const int n = a.tf.n_fits * a.tf.nbins_max;
-            for (int k = tid; k < n; k += BLOCK) s_tab[k] = __ldg(g + k);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            sm.tab_src = src;
+            sm.tab_ctf = CTF;
         }
     }
     __syncthreads();
 
-    const int vj = blockIdx.x * TILE_Y + (tid % TILE_Y);
-    const int vi = blockIdx.y * TILE_X + (tid / TILE_Y);
+    const int vj = by * TY + (tid % TY);
+    const int vi = bx * TX + (tid / TY);
     const bool active = vi < v.nx && vj < v.ny;
-    const int tx0 = blockIdx.y * TILE_X, tx1 = tx0 + TILE_X;
-    const int ty0 = blockIdx.x * TILE_Y, ty1 = ty0 + TILE_Y;
+    const int tx0 = bx * TX, tx1 = tx0 + TX;
+    const int ty0 = by * TY, ty1 = ty0 + TY;
     const size_t p = active ? (size_t)vi * v.ny + vj : 0;
 
     Ray r;
@@ -104,35 +127,33 @@ __global__ void __launch_bounds__(BLOCK) render_kernel(const ytgb_render_args a,
         st.tcount = counts[p];
     }
     const int4 *rects = reinterpret_cast<const int4 *>(a.rects);
-
-    for (int base = 0; base < a.n_order; base += BLOCK) {
-        // ---- bin the next BLOCK bricks against this block's pixel tile -------
+    const int n_order = a.n_order;
+    for (int base = 0; base < n_order; base += BLOCK) {
         const int k = base + tid;
         bool hit = false;
-        if (k < a.n_order) {
+        if (k < n_order) {
             const int4 rc = __ldg(rects + k);
             hit = rc.x < tx1 && rc.y > tx0 && rc.z < ty1 && rc.w > ty0;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, hit);
         const int lane = tid & 31, wid = tid >> 5;
-        if (lane == 0) s_wsum[wid] = __popc(bal);
+        if (lane == 0) sm.wsum[wid] = __popc(bal);
         __syncthreads();
         int off = 0, nsel = 0;
 #pragma unroll
         for (int q = 0; q < NWARP; q++) {
-            off += q < wid ? s_wsum[q] : 0;
-            nsel += s_wsum[q];
+            off += q < wid ? sm.wsum[q] : 0;
+            nsel += sm.wsum[q];
         }
-        if (hit) s_sel[off + __popc(bal & ((1u << lane) - 1u))] = k;
+        if (hit) sm.sel[off + __popc(bal & ((1u << lane) - 1u))] = k;
         __syncthreads();
-
         for (int j = 0; active && j < nsel; j++) {
-            const int kk = s_sel[j];
+            const int kk = sm.sel[j];
             const int4 rc = __ldg(rects + kk);
             if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
             walk_brick<MODE, CTF>(a, s_tab, r, __ldg(a.order + kk), st);
         }
-        __syncthreads();  // s_sel is rewritten by the next chunk
+        __syncthreads();  // sel / wsum are rewritten by the next pass
     }
 
     if (active) {
@@ -146,12 +167,59 @@ __global__ void __launch_bounds__(BLOCK) render_kernel(const ytgb_render_args a,
         }
     }
     if (a.counters) {
-        if (st.visits) atomicAdd(&s_cnt[0], st.visits);
-        if (st.walks) atomicAdd(&s_cnt[1], st.walks);
-        if (st.guarded) atomicAdd(&s_cnt[3], st.guarded);
-        if (active) atomicAdd(&s_cnt[2], 1ull);
+        if (st.visits) atomicAdd(&sm.cnt[0], st.visits);
+        if (st.walks) atomicAdd(&sm.cnt[1], st.walks);
+        if (st.guarded) atomicAdd(&sm.cnt[3], st.guarded);
+        if (active) atomicAdd(&sm.cnt[2], 1ull);
         __syncthreads();
-        if (tid < 4 && s_cnt[tid]) atomicAdd(a.counters + tid, s_cnt[tid]);
+        if (tid < 4 && sm.cnt[tid]) atomicAdd(a.counters + tid, sm.cnt[tid]);
+    }
+    __syncthreads();
+}
+
+// One view, one tile per block.
+template <int MODE, int CTF, int TS>
+__global__ void __launch_bounds__(BLOCK) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
+                                                       long long *counts) {
+    extern __shared__ float4 s_tab[];
+    __shared__ TileSmem sm;
+    if (threadIdx.x == 0) {
+        sm.tab_src = nullptr;
+        sm.tab_ctf = -1;
+    }
+    __syncthreads();
+    render_tile<MODE, CTF, TS>(a, blockIdx.y, blockIdx.x, s_tab, sm, hashes, counts);
+}
+
+// Many views in one persistent launch: blocks pull (view, tile) work items
+// from a device counter until the batch is drained, so small and large views
+// share the GPU without a launch per view.  Entries are sorted by
+// tile_begin; an item's view is found by binary search.
+template <int MODE, int CTF, int TS>
+__global__ void __launch_bounds__(BLOCK) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
+                                                      int total_tiles, int *queue) {
+    extern __shared__ float4 s_tab[];
+    __shared__ TileSmem sm;
+    if (threadIdx.x == 0) {
+        sm.tab_src = nullptr;
+        sm.tab_ctf = -1;
+    }
+    while (true) {
+        if (threadIdx.x == 0) sm.item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int item = sm.item;
+        __syncthreads();
+        if (item >= total_tiles) break;
+        int lo = 0, hi = n_entries - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&entries[mid].tile_begin) <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const ytgb_batch_entry &e = entries[lo];
+        const int t = item - __ldg(&e.tile_begin);
+        const int ty = __ldg(&e.tiles_y);
+        render_tile<MODE, CTF, TS>(e.args, t / ty, t % ty, s_tab, sm, nullptr, nullptr);
     }
 }
 
@@ -181,7 +249,7 @@ int check_args(const ytgb_render_args *a, bool trace) {
         ytgb_set_error("ytgb_render: per-pixel lens needs px_pos / px_dir");
         return YTGB_ERR_INVALID;
     }
-    if (v.lens != YTGB_LENS_PER_PIXEL && v.lens != YTGB_LENS_PLANE_PARALLEL) {
+    if (v.lens != YTGB_LENS_PER_PIXEL && v.lens != YTGB_LENS_PLANE_PARALLEL && v.lens != YTGB_LENS_PERSPECTIVE) {
         ytgb_set_error("ytgb_render: unknown lens");
         return YTGB_ERR_INVALID;
     }
@@ -196,28 +264,107 @@ int check_args(const ytgb_render_args *a, bool trace) {
     return YTGB_OK;
 }
 
-template <int MODE, int CTF>
-int launch(const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long long *h, long long *c) {
-    dim3 grid((a->view.ny + TILE_Y - 1) / TILE_Y, (a->view.nx + TILE_X - 1) / TILE_X);
-    if (grid.y > 65535) {
-        ytgb_set_error("ytgb_render: image too tall");
+// Transfer-function header checks and the shared-memory bytes its tables take.
+int tf_check(const ytgb_tf &t, size_t *smem) {
+    if (t.n_fits < 0 || t.n_fits > 6 || t.nbins_max < 2 || t.nbins_max > YTGB_TF_MAX_BINS) {
+        ytgb_set_error("inconsistent transfer function header");
         return YTGB_ERR_INVALID;
     }
+    for (int q = 0; q < t.n_fits; q++) {
+        if (t.nbins[q] < 2 || t.nbins[q] > t.nbins_max || t.field_id[q] < 0 || t.field_id[q] > 5 ||
+            t.weight_field_id[q] < -1 || t.weight_field_id[q] > 5 || t.weight_table_id[q] < -1 ||
+            t.weight_table_id[q] >= t.n_fits) {
+            ytgb_set_error("transfer function table ids out of range");
+            return YTGB_ERR_INVALID;
+        }
+    }
+    for (int c = 0; c < 6; c++) {
+        if (t.field_table_ids[c] < 0 || t.field_table_ids[c] > 5) {
+            ytgb_set_error("field_table_ids out of range");
+            return YTGB_ERR_INVALID;
+        }
+    }
+    if (t.ctf_fast && (t.n_fits != 4 || t.nbins[0] != t.nbins_max)) {
+        ytgb_set_error("ctf_fast set on tables that are not a ColorTransferFunction");
+        return YTGB_ERR_INVALID;
+    }
+    *smem = t.ctf_fast ? (size_t)3 * t.nbins_max * sizeof(float4) : (size_t)t.n_fits * t.nbins_max * sizeof(float4);
+    if (*smem > 200 * 1024) {
+        ytgb_set_error("transfer-function tables exceed 200 KB of shared memory");
+        return YTGB_ERR_INVALID;
+    }
+    return YTGB_OK;
+}
+
+template <typename K>
+int set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(render_kernel<MODE, CTF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) {
             ytgb_set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
             return YTGB_ERR_CUDA;
         }
     }
-    render_kernel<MODE, CTF><<<grid, BLOCK, smem, s>>>(*a, h, c);
+    return YTGB_OK;
+}
+
+int launch_status(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
-        ytgb_set_error(std::string("render launch: ") + cudaGetErrorString(e));
+        ytgb_set_error(std::string(what) + ": " + cudaGetErrorString(e));
         return YTGB_ERR_CUDA;
     }
     return YTGB_OK;
+}
+
+template <int MODE, int CTF, int TS>
+int launch(const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long long *h, long long *c) {
+    constexpr int TX = TileShape<TS>::X, TY = TileShape<TS>::Y;
+    dim3 grid((a->view.ny + TY - 1) / TY, (a->view.nx + TX - 1) / TX);
+    if (grid.y > 65535) {
+        ytgb_set_error("ytgb_render: image too tall");
+        return YTGB_ERR_INVALID;
+    }
+    if (int st = set_smem(render_kernel<MODE, CTF, TS>, smem)) return st;
+    render_kernel<MODE, CTF, TS><<<grid, BLOCK, smem, s>>>(*a, h, c);
+    return launch_status("render launch");
+}
+
+template <int MODE, int CTF>
+int launch_ts(int ts, const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long long *h, long long *c) {
+    switch (ts) {
+    case 1: return launch<MODE, CTF, 1>(a, smem, s, h, c);
+    case 2: return launch<MODE, CTF, 2>(a, smem, s, h, c);
+    default: return launch<MODE, CTF, 0>(a, smem, s, h, c);
+    }
+}
+
+int tile_shape_of(uint32_t flags) { return (int)((flags >> YTGB_FLAG_TILE_SHIFT) & 0xfu); }
+
+template <int MODE, int CTF, int TS>
+int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem, cudaStream_t s) {
+    if (int st = set_smem(batch_kernel<MODE, CTF, TS>, smem)) return st;
+    if (blocks <= 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, CTF, TS>, BLOCK, smem);
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    if (blocks > total) blocks = total;
+    if (blocks < 1) blocks = 1;
+    batch_kernel<MODE, CTF, TS><<<blocks, BLOCK, smem, s>>>(d, n, total, queue);
+    return launch_status("batch launch");
+}
+
+template <int MODE, int CTF>
+int batch_launch_ts(int ts, const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem,
+                    cudaStream_t s) {
+    switch (ts) {
+    case 1: return batch_launch_t<MODE, CTF, 1>(d, n, total, queue, blocks, smem, s);
+    case 2: return batch_launch_t<MODE, CTF, 2>(d, n, total, queue, blocks, smem, s);
+    default: return batch_launch_t<MODE, CTF, 0>(d, n, total, queue, blocks, smem, s);
+    }
 }
 
 }  // namespace
@@ -226,43 +373,21 @@ extern "C" int ytgb_render(const ytgb_render_args *a, void *stream) {
     int st = check_args(a, false);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    const int ts = tile_shape_of(a->flags);
+    if (ts > 2) {
+        ytgb_set_error("ytgb_render: unknown tile shape");
+        return YTGB_ERR_INVALID;
+    }
     if (a->kind == YTGB_VOLUME_RENDER) {
-        const ytgb_tf &t = a->tf;
-        if (t.n_fits < 0 || t.n_fits > 6 || t.nbins_max < 2 || t.nbins_max > YTGB_TF_MAX_BINS) {
-            ytgb_set_error("ytgb_render: inconsistent transfer function header");
-            return YTGB_ERR_INVALID;
-        }
-        for (int q = 0; q < t.n_fits; q++) {
-            if (t.nbins[q] < 2 || t.nbins[q] > t.nbins_max || t.field_id[q] < 0 || t.field_id[q] > 5 ||
-                t.weight_field_id[q] < -1 || t.weight_field_id[q] > 5 || t.weight_table_id[q] < -1 ||
-                t.weight_table_id[q] >= t.n_fits) {
-                ytgb_set_error("ytgb_render: transfer function table ids out of range");
-                return YTGB_ERR_INVALID;
-            }
-        }
-        for (int c = 0; c < 6; c++) {
-            if (t.field_table_ids[c] < 0 || t.field_table_ids[c] > 5) {
-                ytgb_set_error("ytgb_render: field_table_ids out of range");
-                return YTGB_ERR_INVALID;
-            }
-        }
-        if (t.ctf_fast && (t.n_fits != 4 || t.nbins[0] != t.nbins_max)) {
-            ytgb_set_error("ytgb_render: ctf_fast set on tables that are not a ColorTransferFunction");
-            return YTGB_ERR_INVALID;
-        }
-        const size_t smem = t.ctf_fast ? (size_t)3 * t.nbins_max * sizeof(float4)
-                                       : (size_t)t.n_fits * t.nbins_max * sizeof(float4);
-        if (smem > 200 * 1024) {
-            ytgb_set_error("ytgb_render: transfer-function tables exceed 200 KB of shared memory");
-            return YTGB_ERR_INVALID;
-        }
-        return t.ctf_fast ? launch<MODE_VR, 1>(a, smem, s, nullptr, nullptr)
-                          : launch<MODE_VR, 0>(a, smem, s, nullptr, nullptr);
+        size_t smem = 0;
+        if ((st = tf_check(a->tf, &smem))) return st;
+        return a->tf.ctf_fast ? launch_ts<MODE_VR, 1>(ts, a, smem, s, nullptr, nullptr)
+                              : launch_ts<MODE_VR, 0>(ts, a, smem, s, nullptr, nullptr);
     }
     switch (a->kind) {
-    case YTGB_PROJECTION: return launch<MODE_PROJ, 0>(a, 0, s, nullptr, nullptr);
-    case YTGB_INTERPOLATED_PROJECTION: return launch<MODE_IPROJ, 0>(a, 0, s, nullptr, nullptr);
-    default: return launch<MODE_MIP, 0>(a, 0, s, nullptr, nullptr);
+    case YTGB_PROJECTION: return launch_ts<MODE_PROJ, 0>(ts, a, 0, s, nullptr, nullptr);
+    case YTGB_INTERPOLATED_PROJECTION: return launch_ts<MODE_IPROJ, 0>(ts, a, 0, s, nullptr, nullptr);
+    default: return launch_ts<MODE_MIP, 0>(ts, a, 0, s, nullptr, nullptr);
     }
 }
 
@@ -273,7 +398,74 @@ extern "C" int ytgb_trace(const ytgb_render_args *a, unsigned long long *hashes,
         ytgb_set_error("ytgb_trace: null hash / count arrays");
         return YTGB_ERR_INVALID;
     }
-    return launch<MODE_TRACE, 0>(a, 0, (cudaStream_t)stream, hashes, counts);
+    return launch<MODE_TRACE, 0, 0>(a, 0, (cudaStream_t)stream, hashes, counts);
+}
+
+extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t tile_shape, int32_t *total_tiles,
+                               int32_t *smem_bytes) {
+    if (!entries || n <= 0 || !total_tiles || !smem_bytes || tile_shape < 0 || tile_shape > 2) {
+        ytgb_set_error("ytgb_batch_plan: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    const int TX = tile_shape == 1 ? 16 : (tile_shape == 2 ? 4 : 8);
+    const int TY = BLOCK / TX;
+    const int kind = entries[0].args.kind;
+    const int ctf = kind == YTGB_VOLUME_RENDER ? entries[0].args.tf.ctf_fast : 0;
+    long long total = 0;
+    size_t smem = 0;
+    for (int32_t k = 0; k < n; k++) {
+        ytgb_render_args &a = entries[k].args;
+        if (int st = check_args(&a, false)) return st;
+        if (a.kind != kind || (kind == YTGB_VOLUME_RENDER && a.tf.ctf_fast != ctf)) {
+            ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler and table layout");
+            return YTGB_ERR_INVALID;
+        }
+        if (kind == YTGB_VOLUME_RENDER) {
+            size_t sm = 0;
+            if (int st = tf_check(a.tf, &sm)) return st;
+            smem = sm > smem ? sm : smem;
+        }
+        const int tx = (a.view.nx + TX - 1) / TX, ty = (a.view.ny + TY - 1) / TY;
+        entries[k].tile_begin = (int32_t)total;
+        entries[k].tiles_y = ty;
+        entries[k].tiles = tx * ty;
+        total += (long long)tx * ty;
+        if (total > 0x7fffffff) {
+            ytgb_set_error("ytgb_batch_plan: too many tiles");
+            return YTGB_ERR_INVALID;
+        }
+    }
+    *total_tiles = (int32_t)total;
+    *smem_bytes = (int32_t)smem;
+    return YTGB_OK;
+}
+
+extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+                                 int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
+                                 int32_t blocks, void *stream) {
+    if (!d_entries || n <= 0 || total_tiles <= 0 || !d_queue || tile_shape < 0 || tile_shape > 2 || kind < 0 ||
+        kind > 3 || smem_bytes < 0 || smem_bytes > 200 * 1024) {
+        ytgb_set_error("ytgb_batch_render: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_batch_render: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    const size_t smem = (size_t)smem_bytes;
+    switch (kind) {
+    case YTGB_VOLUME_RENDER:
+        return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s)
+                        : batch_launch_ts<MODE_VR, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s);
+    case YTGB_PROJECTION:
+        return batch_launch_ts<MODE_PROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
+    case YTGB_INTERPOLATED_PROJECTION:
+        return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
+    default:
+        return batch_launch_ts<MODE_MIP, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
+    }
 }
 
 extern "C" int ytgb_check_error(const int32_t *d_error, void *stream) {

@@ -27,7 +27,12 @@ class Renderer:
         self.counters = torch.zeros(4, dtype=torch.int64, device=self.device)
         self.error = torch.zeros(1, dtype=torch.int32, device=self.device)
 
-    def view_args(self, camera):
+    def view_args(self, camera, device_rays=True):
+        """(view, per-pixel positions, per-pixel directions); with
+        ``device_rays`` perspective rays are generated in the kernel and the
+        arrays are None."""
+        if device_rays:
+            return camera.device_view(), None, None
         p = camera.sampler_params()
         nx, ny = camera.resolution
         view, ppos, pdir = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
@@ -40,8 +45,8 @@ class Renderer:
         return self.kdtree.viewpoint_order(camera.viewpoint)
 
     def render(self, camera, kind=_lib.VOLUME_RENDER, n_samples=1, order=None, image=None, zbuffer=None,
-               flags=0, stream=None, keep=None):
-        view, ppos, pdir = self.view_args(camera)
+               flags=0, stream=None, keep=None, device_rays=True):
+        view, ppos, pdir = self.view_args(camera, device_rays)
         nx, ny = camera.resolution
         if order is None:
             order = self.order(camera)
@@ -64,8 +69,8 @@ class Renderer:
         s = torch.cuda.current_stream(self.device)
         _lib.check(_lib.lib().ytgb_check_error(self.error.data_ptr(), s.cuda_stream), "render")
 
-    def trace(self, camera, order=None):
-        view, ppos, pdir = self.view_args(camera)
+    def trace(self, camera, order=None, device_rays=True):
+        view, ppos, pdir = self.view_args(camera, device_rays)
         if order is None:
             order = self.order(camera)
         px_pos = px_dir = None

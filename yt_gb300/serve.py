@@ -1,0 +1,175 @@
+"""A render server: resident volumes, continuous batching, latency accounting.
+
+Volumes (``BrickSet``) and transfer functions (packed tables) stay resident
+in HBM.  Requests -- (volume, transfer function, camera, sampler) -- arrive
+over time.  The loop:
+
+* **admits** arrived requests while their output images fit the HBM budget
+  (a request waits in the arrival queue otherwise);
+* **batches** every admitted, not yet launched request into one
+  :class:`~yt_gb300.batch.Batch` (one persistent launch per sampler class)
+  as soon as one of ``slots`` CUDA streams is free -- so requests that arrive
+  while earlier batches are on the GPU start on another stream at once and
+  their work overlaps on the device (continuous batching, not a queue in
+  front of one stream);
+* **retires** a batch when its completion event fires, frees its images'
+  budget and records each request's latency (completion - arrival).
+
+Each request's image is exactly what rendering it alone gives (the same
+per-ray code, independent of the batch it lands in).
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .batch import Batch, Job
+from .render import Renderer
+
+
+@dataclass
+class Request:
+    rid: int
+    volume: str
+    tf: str
+    camera: object
+    kind: int = _lib.VOLUME_RENDER
+    arrival: float = 0.0          # seconds after the server's start
+    n_samples: int = 1
+    admitted: float = -1.0
+    launched: float = -1.0
+    done: float = -1.0
+    image: torch.Tensor | None = None
+    samples: int = 0
+
+    @property
+    def image_bytes(self) -> int:
+        nx, ny = self.camera.resolution
+        return nx * ny * 4 * 8
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+@dataclass
+class _InFlight:
+    batch: Batch
+    requests: list
+    event: torch.cuda.Event
+    stream: torch.cuda.Stream
+    bytes: int
+    counters: torch.Tensor = field(default=None)
+
+
+class RenderServer:
+    def __init__(self, volumes: dict, tfs: dict, device="cuda", hbm_budget=8 << 30, slots=4, max_batch=64,
+                 tile_shape=0, keep_images=False):
+        """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name -> transfer function."""
+        self.device = torch.device(device)
+        self.renderers = {}
+        self.volumes = {}
+        from .transfer_functions import pack
+        from .volume import BrickSet
+
+        for name, (bricks, kd) in volumes.items():
+            self.volumes[name] = (BrickSet(bricks, device=self.device), kd)
+        self.tfs = {name: (tf, pack(tf)) for name, tf in tfs.items()}
+        self.budget = int(hbm_budget)
+        self.in_use = 0
+        self.slots = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.max_batch = max_batch
+        self.tile_shape = tile_shape
+        self.keep_images = keep_images
+        self.samples = 0
+
+    def renderer(self, volume: str, tf: str | None) -> Renderer:
+        key = (volume, tf)
+        r = self.renderers.get(key)
+        if r is None:
+            bricks, kd = self.volumes[volume]
+            r = Renderer(bricks, None, device=self.device, kdtree=kd)
+            if tf is not None:
+                r.tf, r.packed = self.tfs[tf]
+            self.renderers[key] = r
+        return r
+
+    def _launch(self, reqs, stream, now):
+        jobs = []
+        for q in reqs:
+            q.image = torch.empty((*q.camera.resolution, 4), dtype=torch.float64, device=self.device)
+            r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
+            jobs.append(Job(r, q.camera, q.kind, q.n_samples, q.image))
+        b = Batch(jobs, device=self.device, tile_shape=self.tile_shape)
+        stream.wait_stream(torch.cuda.current_stream(self.device))
+        b.launch(stream)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        for q in reqs:
+            q.launched = now
+        return _InFlight(b, reqs, ev, stream, sum(q.image_bytes for q in reqs))
+
+    def run(self, requests, realtime=True, timeout=600.0):
+        """Serve ``requests`` (sorted by arrival).  With ``realtime`` the
+        arrival times are honoured against the wall clock; otherwise every
+        request is available at once.  Returns the requests with their
+        timings filled in."""
+        pending = deque(sorted(requests, key=lambda q: q.arrival))
+        admitted = deque()
+        inflight: list[_InFlight] = []
+        free = list(self.slots)
+        t0 = time.perf_counter()
+        done = []
+        while pending or admitted or inflight:
+            now = time.perf_counter() - t0
+            if now > timeout:
+                raise TimeoutError("render server: requests not finished in time")
+            # retire finished batches
+            for f in list(inflight):
+                if f.event.query():
+                    t = time.perf_counter() - t0
+                    for q in f.requests:
+                        q.done = t
+                        if not self.keep_images:
+                            q.image = None
+                    self.in_use -= f.bytes
+                    self.samples += int(f.batch.counters[0].item())
+                    f.batch.check()
+                    free.append(f.stream)
+                    inflight.remove(f)
+                    done += f.requests
+            # admit arrivals within the HBM budget
+            while pending and (not realtime or pending[0].arrival <= now):
+                q = pending[0]
+                if q.image_bytes > self.budget:
+                    raise ValueError(f"request {q.rid} needs more than the whole HBM budget")
+                if self.in_use + q.image_bytes > self.budget:
+                    break
+                pending.popleft()
+                q.admitted = now
+                self.in_use += q.image_bytes
+                admitted.append(q)
+            # launch everything admitted on a free slot
+            if admitted and free:
+                reqs = [admitted.popleft() for _ in range(min(self.max_batch, len(admitted)))]
+                inflight.append(self._launch(reqs, free.pop(), now))
+                continue
+            if not admitted and inflight and (not pending or pending[0].arrival > now):
+                # nothing to launch: wait briefly for arrivals or completions
+                nxt = pending[0].arrival - now if pending else 1e-3
+                time.sleep(max(0.0, min(nxt, 2e-4)))
+            elif admitted and not free:
+                time.sleep(5e-5)
+        torch.cuda.synchronize(self.device)
+        return done
+
+
+def latency_summary(reqs):
+    lat = np.array([q.latency for q in reqs]) * 1e3
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "n": int(lat.size)}
