@@ -39,7 +39,7 @@ BYTES_PER_RAY = 64      # float64 RGBA read + written per ray
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", type=int, default=1024)
@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--cpu-res", type=int, default=0, help="resolution of the CPU-baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="amr_vr", choices=["amr_vr", "multiview", "projection", "serve"],
+                    help="amr_vr (default, the headline frame); the others print their own line")
+    ap.add_argument("--tile-shape", type=int, default=-1, help="-1: from the autotuning table")
+    ap.add_argument("--n-requests", type=int, default=2000)
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000")
     return ap.parse_args()
 
 
@@ -80,7 +85,7 @@ class ClockSampler:
                 ["nvidia-smi", f"--id={self.index}",
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
@@ -368,9 +373,290 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _timed_events(fn, steps, stream):
+    import torch
+
+    ts = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        ts.append((e0, e1))
+    torch.cuda.synchronize()
+    return np.array([a.elapsed_time(b) for a, b in ts])
+
+
+def run_multiview(args):
+    """64 cameras on a Fibonacci sphere over a 4-level AMR volume (~4000
+    bricks, 8^3-32^3), image sizes from {128,256,512,1024}^2, half volume
+    rendering and half interpolated projection: 64 sequential single-view
+    launches against one batched persistent launch per sampler class
+    replayed from a CUDA graph."""
+    import torch
+
+    from yt_gb300 import _lib, workloads
+    from yt_gb300.amr_kdtree import AMRKDTree
+    from yt_gb300.batch import Batch, Job
+    from yt_gb300.render import Renderer
+
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    w = workloads.multiview()
+    lin = AMRKDTree(w.kdtree.grids, log_field=False)
+    r_vr = Renderer(w.bricks, w.tf, device=dev, kdtree=w.kdtree)
+    r_pj = Renderer(lin.bricks(), None, device=dev, kdtree=lin)
+    t_build = time.time() - t0
+    ts = args.tile_shape if args.tile_shape >= 0 else 0
+    jobs = [Job(r_vr if v.kind == _lib.VOLUME_RENDER else r_pj, v.camera, v.kind) for v in w.views]
+    stream = torch.cuda.current_stream(dev)
+    # plain: one launch per view, inputs resident (orders and rects prepared)
+    from yt_gb300.volume import render as vrender
+
+    prepared = []
+    for j in jobs:
+        rr = j.renderer
+        view = j.camera.device_view()
+        order = rr.order(j.camera)
+        rects = rr.bricks.rects(view, order)
+        img = torch.zeros((*j.camera.resolution, 4), dtype=torch.float64, device=dev)
+        prepared.append((rr, view, order, rects, img, j.kind))
+    keep = []
+
+    def plain():
+        for rr, view, order, rects, img, kind in prepared:
+            img.zero_()
+            vrender(rr.bricks, view, order, kind, img, tf=rr.packed if kind == _lib.VOLUME_RENDER else None,
+                    counters=rr.counters, error=rr.error, stream=stream, rects=rects, keep=keep,
+                    flags=ts << _lib.FLAG_TILE_SHIFT)
+
+    b = Batch(jobs, device=dev, tile_shape=ts)
+    graph = b.capture()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        plain()
+        graph.replay()
+    torch.cuda.synchronize()
+    keep.clear()
+    r_vr.counters.zero_()
+    r_pj.counters.zero_()
+    b.counters.zero_()
+    ms_plain, ms_batch = [], []
+    clocks = ClockSampler(0)
+    with clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            ms_plain.append(_timed_events(plain, 1, stream)[0])
+            flush.fill_(1.0)
+            ms_batch.append(_timed_events(graph.replay, 1, stream)[0])
+    keep.clear()
+    samples_plain = int(r_vr.counters[0].item() + r_pj.counters[0].item()) // args.steps
+    samples_batch = int(b.counters[0].item()) // args.steps
+    ms_plain, ms_batch = np.array(ms_plain), np.array(ms_batch)
+    hbm, _ = peaks()
+    rays = sum(int(np.prod(j.camera.resolution)) for j in jobs)
+    alg = samples_batch * BYTES_PER_SAMPLE + rays * BYTES_PER_RAY
+    line = {"metric": "Gsamples/s", "workload": "multiview", "value": samples_batch / (ms_batch.mean() / 1e3) / 1e9,
+            "unit": "Gsamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(ms_batch.mean()), "higher_is_better": True,
+            "plain": {"value": samples_plain / (ms_plain.mean() / 1e3) / 1e9, "ms_per_step": float(ms_plain.mean()),
+                      "p50_ms": float(np.percentile(ms_plain, 50)), "p99_ms": float(np.percentile(ms_plain, 99)),
+                      "launches": len(jobs)},
+            "batched": {"p50_ms": float(np.percentile(ms_batch, 50)), "p99_ms": float(np.percentile(ms_batch, 99)),
+                        "launches_per_graph": len(b.groups), "work_items": b.total_tiles, "tile_shape": ts},
+            "samples_per_step": samples_batch, "samples_match": samples_batch == samples_plain,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_batch.mean() / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": alg / (ms_batch.mean() / 1e3) / 1e9 / hbm},
+            "config": {"workload": "64 Fibonacci-sphere cameras, perspective, sizes {128..1024}^2, VR + "
+                                   "interpolated projection, 4-level AMR", "bricks": len(w.bricks),
+                       "grids": w.info["grids"], "rays": rays, "l2": "flushed between steps"},
+            "clocks": clocks.summary(), "build_seconds": t_build}
+    print(json.dumps(line), flush=True)
+
+
+def run_projection(args):
+    """The precision study: a 512^3 float32 lognormal random field,
+    ProjectionSampler and MIP at 2048^2 and three orientations, float32
+    accumulation with and without compensation, each image's max and RMS
+    relative error against the float64 oracle."""
+    import torch
+
+    from oracle import cpu as ocpu
+    from yt_gb300 import _lib, workloads
+    from yt_gb300.render import Renderer, relative_error
+
+    dev = torch.device("cuda", 0)
+    n = args.root if args.root != 128 else 512
+    res = args.res if args.res != 1024 else 2048
+    w = workloads.projection_study(n=n, res=res)
+    field64 = [w.bricks[0][0][0].astype(np.float64)]
+    r = Renderer(w.bricks, None, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    views = []
+    for v in w.views:
+        for comp in (True, False):
+            flags = 0 if comp else _lib.FLAG_NO_COMPENSATION
+            r.counters.zero_()
+            img = torch.zeros((res, res, 4), dtype=torch.float64, device=dev)
+
+            def step():
+                img.zero_()
+                r.render(v.camera, kind=v.kind, image=img, flags=flags)
+
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            r.counters.zero_()
+            ms = _timed_events(step, args.steps, stream)
+            samples = int(r.counters[0].item()) // args.steps
+            out = img.cpu().numpy()
+            entry = {"kind": "projection" if v.kind == _lib.PROJECTION else "mip",
+                     "angle_deg": float(np.rad2deg(np.arctan2(v.camera.unit_vectors[2][1],
+                                                              v.camera.unit_vectors[2][2]))),
+                     "compensated": comp, "ms": float(ms.mean()), "Gsamples/s": samples / (ms.mean() / 1e3) / 1e9,
+                     "cell_visits": samples}
+            views.append((v, comp, entry, out))
+    # float64 oracle per view (shared by both precisions)
+    threads = os.cpu_count() or 1
+    oracle_imgs = {}
+    t_or = 0.0
+    for v, comp, entry, out in views:
+        key = id(v)
+        if key not in oracle_imgs:
+            p = v.camera.sampler_params()
+            s = ocpu.OracleSampler("projection" if v.kind == _lib.PROJECTION else "mip", p["vp_pos"], p["vp_dir"],
+                                   p["center"], p["bounds"], p["image"], p["x_vec"], p["y_vec"], p["width"],
+                                   lens_type=p["lens_type"], camera_data=p["camera_data"])
+            t = time.perf_counter()
+            s.render(ocpu.OracleBricks([(field64, None, np.zeros(3), np.ones(3), [n, n, n])]), None,
+                     num_threads=threads)
+            t_or += time.perf_counter() - t
+            oracle_imgs[key] = p["image"]
+        mx, rms = relative_error(out, oracle_imgs[key], channels=(0,))
+        entry["max_rel_err"], entry["rms_rel_err"] = mx, rms
+    ents = [e for _, _, e, _ in views]
+    comp_ents = [e for e in ents if e["compensated"]]
+    tot_s = sum(e["cell_visits"] for e in comp_ents)
+    tot_ms = sum(e["ms"] for e in comp_ents)
+    hbm, _ = peaks()
+    line = {"metric": "Gsamples/s", "workload": "projection", "value": tot_s / (tot_ms / 1e3) / 1e9,
+            "unit": "Gsamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot_ms, "higher_is_better": True, "views": ents,
+            "roofline": {"bound": "hbm", "achieved": (tot_s * 4 + len(comp_ents) * res * res * 64) / (tot_ms / 1e3) / 1e9,
+                         "peak": hbm, "unit": "GB/s", "model": "4 B/cell visit + 64 B/ray"},
+            "cpu_oracle_seconds": t_or, "cpu_threads": threads,
+            "config": {"workload": f"{n}^3 float32 lognormal GRF (P(k)~k^-3, seed 1), 2048^2 plane-parallel, "
+                                   "angles 0/30/57 deg about x, ProjectionSampler + MIP", "resolution": res}}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Served rendering: four resident volumes (the uniform, AMR, random-field
+    and multi-view datasets, float32 on the device) and 16 transfer
+    functions; Poisson request streams at each rate, each request a random
+    volume, transfer function, camera and size from {256,512,1024,2048}^2;
+    p50/p99 latency, Gsamples/s and the relative error of a 1% audit
+    sample against the float64 oracle."""
+    import torch
+
+    from oracle import cpu as ocpu
+    from yt_gb300 import _lib, testing, workloads
+    from yt_gb300.camera import Camera
+    from yt_gb300.render import relative_error
+    from yt_gb300.serve import RenderServer, Request, latency_summary
+
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    w1 = workloads.uniform_vr()
+    w2 = workloads.amr_vr()
+    w3 = workloads.projection_study(n=256, res=256, angles=(0.0,))
+    w4 = workloads.multiview(n_cams=1)
+    vols = {"uniform": (w1.bricks, w1.kdtree), "amr": (w2.bricks, w2.kdtree), "grf": (w3.bricks, None),
+            "multiview": (w4.bricks, w4.kdtree)}
+    rng = np.random.default_rng(5)
+    tfs = {}
+    for k in range(16):
+        lo, hi = sorted(rng.uniform(-0.3, 1.6, 2))
+        tfs[f"tf{k}"] = workloads.color_tf((lo - 0.2, hi + 0.2), int(rng.integers(3, 9)))
+    srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=4, max_batch=64)
+    t_build = time.time() - t0
+    sizes = (256, 512, 1024, 2048)
+
+    def make(n, rate, seed):
+        rr = np.random.default_rng(seed)
+        t = 0.0
+        out = []
+        for i in range(n):
+            t += rr.exponential(1.0 / rate)
+            vol = str(rr.choice(list(vols)))
+            p = testing.fibonacci_sphere(1, radius=1.0)[0] + rr.normal(0, 0.4, 3)
+            res = int(rr.choice(sizes))
+            if vol == "grf":
+                cam = Camera(p, (0.5, 0.5, 0.5), 1.0, res, lens_type="plane-parallel")
+                kind = _lib.PROJECTION if rr.random() < 0.5 else _lib.MIP
+                out.append(Request(i, vol, None, cam, kind, arrival=t))
+            else:
+                cam = Camera(p, (0.5, 0.5, 0.5), 1.5, res, lens_type="perspective")
+                out.append(Request(i, vol, f"tf{int(rr.integers(16))}", cam, _lib.VOLUME_RENDER, arrival=t))
+        return out
+
+    # warm-up: compile paths, stage tables
+    srv.run(make(16, 1e6, 99), realtime=False)
+    results = []
+    rates = [float(x) for x in args.rates.split(",")]
+    total_samples = 0
+    total_busy = 0.0
+    audit = []
+    for k, rate in enumerate(rates):
+        reqs = make(args.n_requests, rate, 1000 + k)
+        srv.samples = 0
+        t = time.perf_counter()
+        done = srv.run(reqs, realtime=True)
+        wall = time.perf_counter() - t
+        lat = latency_summary(done)
+        results.append({"rate_req_s": rate, **lat, "Gsamples/s": srv.samples / wall / 1e9,
+                        "wall_s": wall, "samples": srv.samples})
+        total_samples += srv.samples
+        total_busy += wall
+        audit += [q for q in done if q.rid % 100 == 0]
+    # 1% audit against the float64 oracle (smallest images of the audit set)
+    audit = sorted(audit, key=lambda q: np.prod(q.camera.resolution))[:8]
+    errs = []
+    for q in audit:
+        srv.keep_images = True
+        img = srv.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None).render(
+            q.camera, kind=q.kind).cpu().numpy()
+        bricks, kd = vols[q.volume]
+        if q.kind != _lib.VOLUME_RENDER:
+            bricks = [([bricks[0][0][0].astype(np.float64)], None, bricks[0][2], bricks[0][3], bricks[0][4])]
+        p = q.camera.sampler_params()
+        name = {0: "volume_render", 1: "projection", 3: "mip"}[q.kind]
+        s = ocpu.OracleSampler(name, p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"], p["x_vec"],
+                               p["y_vec"], p["width"], lens_type=p["lens_type"], camera_data=p["camera_data"],
+                               tf=tfs[q.tf] if q.tf else None)
+        order = kd.viewpoint_order(q.camera.viewpoint) if kd is not None else None
+        s.render(ocpu.OracleBricks(bricks), order, num_threads=os.cpu_count() or 1)
+        errs.append(relative_error(img, p["image"], channels=(0, 1, 2) if q.kind == 0 else (0,))[0])
+    line = {"metric": "Gsamples/s & p50/p99 latency", "workload": "serve",
+            "value": total_samples / total_busy / 1e9, "unit": "Gsamples/s", "n_gpus": 1,
+            "higher_is_better": True, "rates": results,
+            "audit": {"n": len(errs), "max_rel_err": float(max(errs)) if errs else None},
+            "config": {"volumes": {k: len(v[0]) for k, v in vols.items()}, "tfs": 16, "sizes": list(sizes),
+                       "requests_per_rate": args.n_requests, "slots": 4, "max_batch": 64},
+            "build_seconds": t_build}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "multiview":
+        run_multiview(a)
+    elif a.workload == "projection":
+        run_projection(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)
