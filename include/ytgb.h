@@ -52,21 +52,27 @@ extern "C" {
 #define YTGB_FLAG_TILE_SHIFT 8         /* bits 8..11: tile shape 0 = 8x16, 1 = 16x8, 2 = 4x32 pixels */
 
 /* One brick: the fields of yt's VolumeContainer (volume_container.pxd:13-33,
- * filled by PartitionedGrid.__cinit__, partitioned_grid.pyx:28-63).  The
- * brick's field f occupies data[data_offset + f*field_stride ...] in the
- * float32 arena: (dims+1)^3 vertex values for vertex-centred samplers, dims^3
- * cell values for ProjectionSampler / MIP, C order. */
+ * filled by PartitionedGrid.__cinit__, partitioned_grid.pyx:28-63), plus
+ * per-brick constants of walk_volume precomputed on the host with the same
+ * float64 operations.  The brick's field f occupies
+ * data[data_offset + f*field_stride ...] in the float32 arena: (dims+1)^3
+ * vertex values for vertex-centred samplers, dims^3 cell values for
+ * ProjectionSampler / MIP, C order. */
 typedef struct ytgb_brick {
     double left_edge[3];
     double right_edge[3];
     double dds[3];        /* (right_edge - left_edge) / dims */
     double idds[3];       /* 1 / dds */
+    double snap[3];       /* 1e-10 * dds: face snapping tolerance (grid_traversal.pyx:67-74) */
     int32_t dims[3];
     int32_t n_fields;
     int64_t data_offset;  /* float index of field 0 */
     int64_t field_stride; /* floats between consecutive fields */
     int64_t mask_offset;  /* byte index into the mask arena; -1 = all ones */
-    int64_t pad;
+    int64_t bounds_offset;/* double index of the cell-boundary table (k*dds + le,
+                           * k = 0..dims, per axis: grid_traversal.pyx:106-108) */
+    float lef[3], ref[3], iddsf[3];  /* float32 copies for conservative pre-tests */
+    int32_t pad[5];
 } ytgb_brick;
 
 /* One view: the ray-generation and culling fields of ImageSampler
@@ -126,6 +132,7 @@ typedef struct ytgb_render_args {
     const int32_t *rects;      /* device: 4 per order entry, from ytgb_brick_rects */
     const float *data;         /* device float32 arena */
     const uint8_t *masks;      /* device mask arena, or NULL when all are -1 */
+    const double *bounds;      /* device cell-boundary tables (see ytgb_brick) */
     ytgb_tf tf;                /* by value, from ytgb_tf_pack (VR only) */
     const float *tf_tables;    /* device, VR only */
     double *image;             /* device (nx,ny,4) float64, updated in place */

@@ -74,3 +74,59 @@ extern "C" void emu_rays(const ytgb_view *v, double *pos, double *dir) {
             }
         }
 }
+
+// ---- direct checks of the integer float64 helpers --------------------------
+#include <random>
+static double rand_pos(std::mt19937_64 &g) {
+    // positive doubles over a wide range, with many short mantissas (ties)
+    std::uniform_real_distribution<double> u(-12.0, 2.0);
+    double x = std::pow(2.0, u(g));
+    if (g() % 4 == 0) {
+        long long b;
+        std::memcpy(&b, &x, 8);
+        b &= ~((1LL << (g() % 52)) - 1);  // clear low mantissa bits
+        std::memcpy(&x, &b, 8);
+    }
+    return x;
+}
+
+// returns the number of mismatches of repeated tmax += tdelta (n walks of
+// `steps` additions) between the integer stepping and float64 addition
+extern "C" long long emu_check_step(long long n, int steps, unsigned long long seed) {
+    std::mt19937_64 g(seed);
+    long long bad = 0;
+    for (long long k = 0; k < n; k++) {
+        double x = rand_pos(g), d = rand_pos(g) * std::pow(2.0, -(double)(g() % 30));
+        AxisStep s;
+        s.bits = dbits(x);
+        step_prepare(s, d);
+        double ref = x;
+        for (int j = 0; j < steps; j++) {
+            ref = ref + d;
+            step_advance(s, d);
+            if (s.bits != dbits(ref)) { bad++; break; }
+        }
+    }
+    return bad;
+}
+
+// mismatches of diff_to_float against (float)(x - y) computed in long double
+// (exact for these inputs), and of split_floor against floor / fraction
+extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
+    std::mt19937_64 g(seed);
+    long long bad = 0;
+    for (long long k = 0; k < n; k++) {
+        double y = rand_pos(g), x = y * (1.0 + std::ldexp((double)(g() % 1000000), -(int)(g() % 40)));
+        if (g() % 3 == 0) std::swap(x, y);
+        float got = diff_to_float(dbits(x), dbits(y));
+        float want = (float)((long double)x - (long double)y);
+        if (got != want) bad++;
+        double t = std::ldexp((double)(g() >> 11), -(int)(g() % 60));  // 0 <= t < 2^53 .. small
+        if (t > 0 && t < 1073741824.0) {
+            int fl; float fr;
+            split_floor(dbits(t), fl, fr);
+            if (fl != (int)std::floor(t) || fr != (float)(t - std::floor(t))) bad++;
+        }
+    }
+    return bad;
+}

@@ -168,3 +168,65 @@ def test_sampler_constructor_errors():
                           np.ones(3), np.ones(3), np.ones(3), "Nope", 1, lens_type="plane-parallel")
     with pytest.raises(NotImplementedError):
         s(None)
+
+
+def _args_for(view, n_order=1):
+    a = _lib.RenderArgs()
+    a.kind = _lib.PROJECTION
+    a.n_samples = 1
+    a.n_order = n_order
+    a.view = view
+    buf = np.zeros(64, dtype=np.float64)
+    base = buf.ctypes.data
+    a.bricks = base
+    a.order = base
+    a.rects = base
+    a.data = base
+    a.bounds = base
+    a.image = base
+    return a, buf
+
+
+def test_render_rejects_misaligned_pointers_before_launch():
+    """Host-side guards: a misaligned rects table (read as 16-byte int4) is
+    rejected before any device work (so this runs without a GPU)."""
+    cam = Camera((0.5, 0.5, -1.0), 0.5, 1.0, 8)
+    a, buf = _args_for(cam.device_view())
+    a.rects = buf.ctypes.data + 4
+    st = _lib.lib().ytgb_render(C.byref(a), None)
+    assert st == _lib.ERR_INVALID and b"misaligned" in _lib.lib().ytgb_last_error()
+    a.rects = buf.ctypes.data
+    a.bounds = None
+    assert _lib.lib().ytgb_render(C.byref(a), None) == _lib.ERR_INVALID
+
+
+def test_batch_plan_rejects_misaligned_and_counts_tiles():
+    cam = Camera((0.5, 0.5, -1.0), 0.5, 1.0, (20, 33))
+    e = (_lib.BatchEntry * 2)()
+    a, buf = _args_for(cam.device_view())
+    e[0].args = a
+    e[1].args = a
+    t, s = C.c_int32(), C.c_int32()
+    assert _lib.lib().ytgb_batch_plan(e, 2, 0, C.byref(t), C.byref(s)) == 0
+    per = ((20 + 7) // 8) * ((33 + 15) // 16)
+    assert t.value == 2 * per and e[1].tile_begin == per and e[1].tiles_y == 3
+    e[1].args.rects = buf.ctypes.data + 8
+    assert _lib.lib().ytgb_batch_plan(e, 2, 0, C.byref(t), C.byref(s)) == _lib.ERR_INVALID
+
+
+def test_batch_tables_are_aligned_for_every_view():
+    """Batch packs every view's rects + order into one buffer; each view's
+    rects must start on a 16-byte boundary (ytgb_batch_plan checks it)."""
+    from yt_gb300.batch import Batch, Job
+    from yt_gb300.render import Renderer
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=16)
+    r = Renderer(w.bricks, w.tf, device="cpu", kdtree=w.kdtree)
+    sub = Renderer(w.bricks[:7], w.tf, device="cpu")  # 7 bricks: 35-int tables
+    jobs = [Job(sub, Camera((0.5, 0.5, -1.0), 0.5, 1.2, 12)), Job(r, Camera((1.3, 0.4, -0.6), 0.5, 1.5, 16,
+                                                                           lens_type="perspective")),
+            Job(sub, Camera((0.2, 1.4, 0.3), 0.5, 1.2, (9, 14)))]
+    b = Batch(jobs, device="cpu")
+    for g in b.groups:
+        for k in range(g.n):
+            assert g.entries[k].args.rects % 16 == 0

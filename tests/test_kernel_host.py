@@ -64,6 +64,7 @@ def run_emu(L, bricks, cam, order, kind, tf=None, ns=1, zbuffer=None):
     if ppos is not None:
         a.view.px_pos, a.view.px_dir = ppos.ctypes.data, pdir.ctypes.data
     a.bricks, a.order, a.rects, a.data = bs.desc.data_ptr(), order.ctypes.data, rects.ctypes.data, bs.data.data_ptr()
+    a.bounds = bs.bounds.data_ptr()
     keep = []
     if bs.masks is not None:
         a.masks = bs.masks.data_ptr()
@@ -213,6 +214,7 @@ def test_device_perspective_render_matches_oracle(emu):
     a = _lib.RenderArgs()
     a.kind, a.n_samples, a.n_order, a.view = _lib.VOLUME_RENDER, 1, order.size, view
     a.bricks, a.order, a.rects, a.data = bs.desc.data_ptr(), order.ctypes.data, rects.ctypes.data, bs.data.data_ptr()
+    a.bounds = bs.bounds.data_ptr()
     pk = pack(w.tf)
     a.tf, a.tf_tables = pk.header, pk.tables.ctypes.data
     img = np.zeros((48, 48, 4))
@@ -220,3 +222,18 @@ def test_device_perspective_render_matches_oracle(emu):
     emu.emu_render(C.byref(a), 0, None, None, np.zeros(4, dtype=np.uint64).ctypes.data)
     ref, *_ = run_oracle(w.bricks, cam, order, _lib.VOLUME_RENDER, w.tf)
     assert relative_error(img, ref)[0] <= TOL
+
+
+def test_integer_float64_stepping_matches_dadd(emu):
+    """step_advance (the walk's tmax += tdelta on bit patterns) equals float64
+    addition over 200k random walks of 64 steps, including short mantissas
+    that produce exact half-ulp ties."""
+    emu.emu_check_step.restype = C.c_longlong
+    emu.emu_check_step.argtypes = [C.c_longlong, C.c_int, C.c_ulonglong]
+    assert emu.emu_check_step(200_000, 64, 1) == 0
+
+
+def test_integer_conversions_match(emu):
+    emu.emu_check_convert.restype = C.c_longlong
+    emu.emu_check_convert.argtypes = [C.c_longlong, C.c_ulonglong]
+    assert emu.emu_check_convert(1_000_000, 2) == 0

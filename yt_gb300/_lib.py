@@ -30,12 +30,17 @@ class Brick(C.Structure):
         ("right_edge", C.c_double * 3),
         ("dds", C.c_double * 3),
         ("idds", C.c_double * 3),
+        ("snap", C.c_double * 3),
         ("dims", C.c_int32 * 3),
         ("n_fields", C.c_int32),
         ("data_offset", C.c_int64),
         ("field_stride", C.c_int64),
         ("mask_offset", C.c_int64),
-        ("pad", C.c_int64),
+        ("bounds_offset", C.c_int64),
+        ("lef", C.c_float * 3),
+        ("ref", C.c_float * 3),
+        ("iddsf", C.c_float * 3),
+        ("pad", C.c_int32 * 5),
     ]
 
 
@@ -91,6 +96,7 @@ class RenderArgs(C.Structure):
         ("rects", C.c_void_p),
         ("data", C.c_void_p),
         ("masks", C.c_void_p),
+        ("bounds", C.c_void_p),
         ("tf", TF),
         ("tf_tables", C.c_void_p),
         ("image", C.c_void_p),

@@ -71,7 +71,11 @@ class Batch:
             from .volume import check_inputs
 
             check_inputs(j.renderer.bricks, view, order, j.kind, j.image)
-            tables.append(np.concatenate([rects.ravel(), order]).astype(np.int32))
+            # rects are read as 16-byte int4: every view's table starts on a
+            # 16-byte boundary of the shared buffer
+            t = np.concatenate([rects.ravel(), order]).astype(np.int32)
+            pad = (-t.size) % 4
+            tables.append(np.concatenate([t, np.zeros(pad, dtype=np.int32)]) if pad else t)
             views.append((view, order.size))
         offs = np.cumsum([0] + [t.size for t in tables])
         self.tables = torch.from_numpy(np.concatenate(tables)).to(self.device)
@@ -92,6 +96,7 @@ class Batch:
             a.rects = base + 4 * int(off)
             a.order = base + 4 * (int(off) + 4 * n_order)
             a.data = j.renderer.bricks.data.data_ptr()
+            a.bounds = j.renderer.bricks.bounds.data_ptr()
             a.masks = j.renderer.bricks.masks.data_ptr() if j.renderer.bricks.masks is not None else None
             if tf is not None:
                 a.tf = tf.header

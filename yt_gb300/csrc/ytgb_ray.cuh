@@ -81,6 +81,137 @@ YTGB_HD long long dkey(double x) {
     return (b ^ (m & 0x7fffffffffffffffll)) - m;
 }
 
+
+// ---- integer-exact helpers for positive float64 values --------------------
+// These replace float64-pipe instructions (conversions, floor, the walk's
+// `tmax += tdelta`) by integer work on the bit patterns, with identical
+// results.
+constexpr long long MANT52 = (1LL << 52) - 1;
+
+#ifdef __CUDA_ARCH__
+YTGB_HD double dfrom(long long b) { return __longlong_as_double(b); }
+YTGB_HD int clz64(unsigned long long x) { return __clzll((long long)x); }
+YTGB_HD float ffrom(uint32_t b) { return __uint_as_float(b); }
+#else
+YTGB_HD double dfrom(long long b) {
+    double x;
+    std::memcpy(&x, &b, sizeof(x));
+    return x;
+}
+YTGB_HD int clz64(unsigned long long x) { return __builtin_clzll(x); }
+YTGB_HD float ffrom(uint32_t b) {
+    float x;
+    std::memcpy(&x, &b, sizeof(x));
+    return x;
+}
+#endif
+
+// The float nearest to F * 2^k (round to nearest even), F > 0 or 0.
+YTGB_HD float scaled_to_float(unsigned long long F, int k) {
+    if (F == 0) return 0.0f;
+    const int lead = 63 - clz64(F);
+    int e = lead + k;
+    unsigned long long sig;
+    if (lead > 23) {
+        const int rs = lead - 23;
+        sig = F >> rs;
+        const unsigned long long rem = F & ((1ull << rs) - 1), half = 1ull << (rs - 1);
+        if (rem > half || (rem == half && (sig & 1ull))) {
+            sig++;
+            if (sig == (1ull << 24)) {
+                sig >>= 1;
+                e++;
+            }
+        }
+    } else {
+        sig = F << (23 - lead);
+    }
+    if (e > 127) return ffrom(0x7f800000u);
+    if (e < -126) return 0.0f;  // below float's normal range: negligible here
+    return ffrom(((uint32_t)(e + 127) << 23) | (uint32_t)(sig & 0x7fffffull));
+}
+
+// x - y as float for x >= y >= 0 given as float64 bit patterns: exact
+// integer difference when the exponents are equal or adjacent, else float64.
+YTGB_HD float diff_to_float_ordered(long long xb, long long yb) {
+    const int ex = (int)(xb >> 52), ey = (int)(yb >> 52);
+    if (ey > 0 && ex == ey) return scaled_to_float((unsigned long long)(xb - yb), ex - 1075);
+    if (ey > 0 && ex == ey + 1) {
+        const unsigned long long mx = (unsigned long long)((xb & MANT52) | (1LL << 52));
+        const unsigned long long my = (unsigned long long)((yb & MANT52) | (1LL << 52));
+        return scaled_to_float(2 * mx - my, ey - 1075);
+    }
+    return (float)dsub(dfrom(xb), dfrom(yb));
+}
+
+// x - y for x, y >= 0 (bit patterns order like the values).  A walk's first
+// dt can be slightly negative: yt's rounded tmax may sit just below a
+// snapped intersect_t.
+YTGB_HD float diff_to_float(long long xb, long long yb) {
+    return xb >= yb ? diff_to_float_ordered(xb, yb) : -diff_to_float_ordered(yb, xb);
+}
+
+// floor(ty) and ty - floor(ty) (as float) for a positive normal ty < 2^30.
+YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
+    const int e = (int)(tb >> 52) - 1023;
+    const unsigned long long m = (unsigned long long)((tb & MANT52) | (1LL << 52));
+    if (e < 0) {
+        fl = 0;
+        frac = scaled_to_float(m, e - 52);
+    } else {
+        const int sh = 52 - e;
+        fl = (int)(m >> sh);
+        frac = scaled_to_float(m & ((1ull << sh) - 1), -sh);
+    }
+}
+
+// fl(x + d) with x, d > 0, repeated for one walk axis.  Inside one binade
+// of x the float64 sum advances x by a fixed number q of ulps (plus one
+// when the discarded part of d exceeds half an ulp; on an exact half, the
+// even neighbour): an integer add on the bit pattern.  Anything else --
+// leaving the binade, d not below x's binade, non-normal operands -- takes
+// the float64 add.
+struct AxisStep {
+    long long bits;  // the float64 bits of tmax
+    long long q;
+    long long end;   // first bit pattern of the next binade
+    int mode;        // 0 round down, 1 round up, 2 half (to even), 3 float64 add
+};
+
+YTGB_HD void step_prepare(AxisStep &s, double d) {
+    const long long xb = s.bits, db = dbits(d);
+    const int ex = (int)(xb >> 52), ed = (int)(db >> 52);
+    s.end = (long long)(ex + 1) << 52;
+    s.q = 0;
+    if (xb <= 0 || db <= 0 || ex == 0 || ed == 0 || ex >= 2046 || ed >= 2047 || ed >= ex) {
+        s.mode = 3;
+        return;
+    }
+    const int sh = ex - ed;
+    if (sh >= 64) {
+        s.mode = 0;
+        return;
+    }
+    const unsigned long long md = (unsigned long long)((db & MANT52) | (1LL << 52));
+    s.q = (long long)(md >> sh);
+    const unsigned long long r = md & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    s.mode = r < half ? 0 : (r > half ? 1 : 2);
+}
+
+YTGB_HD void step_advance(AxisStep &s, double d) {
+    if (s.mode != 3) {
+        long long inc = s.q + (s.mode == 1 ? 1 : 0);
+        if (s.mode == 2) inc += (s.bits + s.q) & 1;
+        const long long nb = s.bits + inc;
+        if (nb < s.end) {
+            s.bits = nb;
+            return;
+        }
+    }
+    s.bits = dbits(dadd(dfrom(s.bits), d));
+    step_prepare(s, d);
+}
+
 struct Ray {
     double pos[3];
     double dir[3];
@@ -137,23 +268,20 @@ YTGB_HD void make_ray(const ytgb_view &v, int vi, int vj, Ray &r) {
     }
 }
 
-struct BrickGeom {
-    double le[3], re[3], dds[3], idds[3];
+// Brick data for the float32 pre-tests (loaded for every candidate brick).
+struct BrickF {
+    float lef[3], ref[3], iddsf[3];
     int dims[3];
 };
 
-YTGB_HD void load_brick(const ytgb_brick *bp, BrickGeom &g) {
-    const double *d = reinterpret_cast<const double *>(bp);
+YTGB_HD void load_brick_f(const ytgb_brick *bp, BrickF &f) {
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        g.le[i] = ldg(d + i);
-        g.re[i] = ldg(d + 3 + i);
-        g.dds[i] = ldg(d + 6 + i);
-        g.idds[i] = ldg(d + 9 + i);
+        f.lef[i] = ldg(&bp->lef[i]);
+        f.ref[i] = ldg(&bp->ref[i]);
+        f.iddsf[i] = ldg(&bp->iddsf[i]);
+        f.dims[i] = ldg(&bp->dims[i]);
     }
-    const int *di = reinterpret_cast<const int *>(d + 12);
-    YTGB_UNROLL
-    for (int i = 0; i < 3; i++) g.dims[i] = ldg(di + i);
 }
 
 // Float32 slab test of the brick's box grown by a margin m (1e-4 of the
@@ -161,11 +289,11 @@ YTGB_HD void load_brick(const ytgb_brick *bp, BrickGeom &g) {
 // and walk_volume's 1e-10*dds face snapping).  True only when the ray misses
 // the grown box for every t in [0, max_t]; then no face test of walk_volume
 // can pass with intersect_t < max_t and the exact set-up returns 0.
-YTGB_HD bool surely_misses(const BrickGeom &b, const Ray &r, float max_t) {
+YTGB_HD bool surely_misses(const BrickF &b, const Ray &r, float max_t) {
     float t0 = -1e30f, t1 = 1e30f;
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        const float lo = (float)b.le[i], hi = (float)b.re[i];
+        const float lo = b.lef[i], hi = b.ref[i];
         const float m = 1e-4f * (fabsf(lo) + fabsf(hi) + fabsf(r.fpos[i]) + 1.0f);
         if (r.step[i] == 0) {
             if (r.fpos[i] < lo - m || r.fpos[i] > hi + m) return true;
@@ -174,7 +302,7 @@ YTGB_HD bool surely_misses(const BrickGeom &b, const Ray &r, float max_t) {
             float ta = (lo - m - r.fpos[i]) * inv;
             float tb = (hi + m - r.fpos[i]) * inv;
             if (ta > tb) {
-                float tmp = ta;
+                const float tmp = ta;
                 ta = tb;
                 tb = tmp;
             }
@@ -194,22 +322,34 @@ struct Walk {
 };
 
 // walk_volume set-up (grid_traversal.pyx:42-118).  Returns false where the
-// reference returns 0 before its loop.
-YTGB_HD bool walk_setup(const BrickGeom &b, const Ray &r, double max_t, Walk &w) {
+// reference returns 0 before its loop.  Every float64 value it keeps is
+// computed from the same operands as the reference; float32 estimates only
+// decide comparisons whose outcome they prove (their margins exceed their
+// error bound by >= 80x), and the index and position of the entry point are
+// read from the bits of the float64 coordinate.
+YTGB_HD bool walk_setup(const BrickF &bf, const ytgb_brick *bp, const double *bounds, const Ray &r, double max_t,
+                        long long kmax, Walk &w) {
+    double le[3], re[3], idds[3];
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        le[i] = ldg(&bp->left_edge[i]);
+        re[i] = ldg(&bp->right_edge[i]);
+        idds[i] = ldg(&bp->idds[i]);
+    }
     int direction = -1;
     double intersect_t = 1.1;
-    // inside test (:44-48); skipped when float32 says the start point is
-    // clearly outside the brick
+    long long kint = dkey(1.1);
+    // inside test (:44-48), exact only when float32 cannot exclude it
     bool maybe_inside = true;
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        const float lo = (float)b.le[i], hi = (float)b.re[i];
-        const float m = 1e-5f * (fabsf(lo) + fabsf(hi) + fabsf(r.fpos[i]) + 1e-3f);
-        maybe_inside = maybe_inside && !(r.fpos[i] < lo - m) && !(r.fpos[i] > hi + m);
+        const float m = 1e-5f * (fabsf(bf.lef[i]) + fabsf(bf.ref[i]) + fabsf(r.fpos[i]) + 1e-3f);
+        maybe_inside = maybe_inside && !(r.fpos[i] < bf.lef[i] - m) && !(r.fpos[i] > bf.ref[i] + m);
     }
-    if (maybe_inside && b.le[0] <= r.pos[0] && r.pos[0] < b.re[0] && b.le[1] <= r.pos[1] && r.pos[1] < b.re[1] &&
-        b.le[2] <= r.pos[2] && r.pos[2] < b.re[2]) {
+    if (maybe_inside && le[0] <= r.pos[0] && r.pos[0] < re[0] && le[1] <= r.pos[1] && r.pos[1] < re[1] &&
+        le[2] <= r.pos[2] && r.pos[2] < re[2]) {
         intersect_t = 0.0;
+        kint = 0;
         direction = 3;
     }
     if (direction != 3) {
@@ -217,72 +357,89 @@ YTGB_HD bool walk_setup(const BrickGeom &b, const Ray &r, double max_t, Walk &w)
         for (int i = 0; i < 3; i++) {
             if (r.step[i] == 0) continue;
             const int x = (i + 1) % 3, y = (i + 2) % 3;
-            // Float32 pre-test of where the ray meets this face's plane.  The
-            // error of q below is at most ~4 float32 roundings of
-            // (|e|+|p_i|)|d_x/d_i| + |tl d_x| + |p_x|; the margin is 1e-5 of
-            // that sum (and of the edges), so a point this far off the face
-            // is off it in float64 as well.  NaN or inf never prunes.
-            {
-                const float e = r.step[i] > 0 ? (float)b.le[i] : (float)b.re[i];
-                const float a0 = fabsf(e) + fabsf(r.fpos[i]);
-                const float tlf = (e - r.fpos[i]) / r.fdir[i];
-                const float qx = r.fpos[x] + tlf * r.fdir[x];
-                const float qy = r.fpos[y] + tlf * r.fdir[y];
-                const float sx = 1e-5f * (a0 * fabsf(r.fdir[x] / r.fdir[i]) + fabsf(tlf * r.fdir[x]) +
-                                          fabsf(r.fpos[x]) + fabsf((float)b.le[x]) + fabsf((float)b.re[x]) + 1e-3f);
-                const float sy = 1e-5f * (a0 * fabsf(r.fdir[y] / r.fdir[i]) + fabsf(tlf * r.fdir[y]) +
-                                          fabsf(r.fpos[y]) + fabsf((float)b.le[y]) + fabsf((float)b.re[y]) + 1e-3f);
-                const float st = 1e-5f * (a0 / fabsf(r.fdir[i]) + fabsf(tlf) + 1e-3f);
-                if (qx < (float)b.le[x] - sx || qx > (float)b.re[x] + sx || qy < (float)b.le[y] - sy ||
-                    qy > (float)b.re[y] + sy || tlf < -st)
-                    continue;
+            // Float32 estimate of where the ray meets this face's plane.  The
+            // error of q is at most ~4 float32 roundings of
+            // (|e|+|p_i|)|d_x/d_i| + |tl d_x| + |p_x| (+ the edges' own
+            // rounding); the margins are 1e-5 of that sum.  NaN or inf never
+            // decides anything.
+            const float e = r.step[i] > 0 ? bf.lef[i] : bf.ref[i];
+            const float a0 = fabsf(e) + fabsf(r.fpos[i]);
+            const float tlf = (e - r.fpos[i]) / r.fdir[i];
+            const float qx = r.fpos[x] + tlf * r.fdir[x];
+            const float qy = r.fpos[y] + tlf * r.fdir[y];
+            const float sx = 1e-5f * (a0 * fabsf(r.fdir[x] / r.fdir[i]) + fabsf(tlf * r.fdir[x]) + fabsf(r.fpos[x]) +
+                                      fabsf(bf.lef[x]) + fabsf(bf.ref[x]) + 1e-3f);
+            const float sy = 1e-5f * (a0 * fabsf(r.fdir[y] / r.fdir[i]) + fabsf(tlf * r.fdir[y]) + fabsf(r.fpos[y]) +
+                                      fabsf(bf.lef[y]) + fabsf(bf.ref[y]) + 1e-3f);
+            const float st = 1e-5f * (a0 / fabsf(r.fdir[i]) + fabsf(tlf) + 1e-3f);
+            if (qx < bf.lef[x] - sx || qx > bf.ref[x] + sx || qy < bf.lef[y] - sy || qy > bf.ref[y] + sy || tlf < -st)
+                continue;  // clearly off the face: the exact test fails too
+            const double tl = r.step[i] > 0 ? dmul(dsub(le[i], r.pos[i]), r.iv[i]) : dmul(dsub(re[i], r.pos[i]), r.iv[i]);
+            const long long ktl = dkey(tl);
+            // the reference's last clause, 0 <= tl < intersect_t, first
+            if (!(ktl >= 0 && ktl < kint)) continue;
+            // clearly inside the face: no snapping and the bounds test holds
+            const bool clear = qx > bf.lef[x] + sx && qx < bf.ref[x] - sx && qy > bf.lef[y] + sy && qy < bf.ref[y] - sy;
+            if (!clear) {
+                double tx = dadd(r.pos[x], dmul(tl, r.dir[x]));
+                double ty = dadd(r.pos[y], dmul(tl, r.dir[y]));
+                const double ex = ldg(&bp->snap[x]), ey = ldg(&bp->snap[y]);
+                if (fabs(dsub(tx, le[x])) < ex) tx = le[x];
+                else if (fabs(dsub(tx, re[x])) < ex) tx = re[x];
+                if (fabs(dsub(ty, le[y])) < ey) ty = le[y];
+                else if (fabs(dsub(ty, re[y])) < ey) ty = re[y];
+                if (!(le[x] <= tx && tx <= re[x] && le[y] <= ty && ty <= re[y])) continue;
             }
-            double tl = r.step[i] > 0 ? dmul(dsub(b.le[i], r.pos[i]), r.iv[i]) : dmul(dsub(b.re[i], r.pos[i]), r.iv[i]);
-            // the last clause of the reference's test, evaluated first (the
-            // clauses have no side effects)
-            if (!(0.0 <= tl && tl < intersect_t)) continue;
-            double tx = dadd(r.pos[x], dmul(tl, r.dir[x]));
-            double ty = dadd(r.pos[y], dmul(tl, r.dir[y]));
-            const double ex = dmul(1e-10, b.dds[x]), ey = dmul(1e-10, b.dds[y]);
-            if (fabs(dsub(tx, b.le[x])) < ex) tx = b.le[x];
-            else if (fabs(dsub(tx, b.re[x])) < ex) tx = b.re[x];
-            if (fabs(dsub(ty, b.le[y])) < ey) ty = b.le[y];
-            else if (fabs(dsub(ty, b.re[y])) < ey) ty = b.re[y];
-            if (b.le[x] <= tx && tx <= b.re[x] && b.le[y] <= ty && ty <= b.re[y]) {
-                direction = i;
-                intersect_t = tl;
-            }
+            direction = i;
+            intersect_t = tl;
+            kint = ktl;
         }
     }
-    if (!((0.0 <= intersect_t) && (intersect_t < max_t))) return false;
+    if (!(kint >= 0 && kint < kmax)) return false;  // !(0 <= intersect_t < max_t)
+    const long long boff = ldg(&bp->bounds_offset);
+    int aoff = 0;
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        double ty = 0.0;
+        const int dims = bf.dims[i];
         if (i == direction && r.step[i] > 0) {
             w.cur[i] = 0;
             w.P[i] = 0.0f;
         } else if (i == direction && r.step[i] < 0) {
-            w.cur[i] = b.dims[i] - 1;
+            w.cur[i] = dims - 1;
             w.P[i] = 1.0f;
         } else {
-            double tx = dadd(dmul(intersect_t, r.dir[i]), r.pos[i]);
-            ty = dmul(dsub(tx, b.le[i]), b.idds[i]);
-            // the sample position keeps the unclamped coordinate: yt's clamps
-            // below only steer the index (its sampler recomputes dp from the
-            // ray, image_samplers.pyx:475-478)
-            const double ty_raw = ty;
-            if (-1 < ty && ty < 0 && r.step[i] > 0) ty = 0.0;
-            else if (b.dims[i] - 1 < ty && ty < b.dims[i] && r.step[i] < 0) ty = (double)(b.dims[i] - 1);
-            w.cur[i] = (int)floor(ty);
-            w.P[i] = (float)dsub(ty_raw, (double)w.cur[i]);
+            const double tx = dadd(dmul(intersect_t, r.dir[i]), r.pos[i]);
+            const double ty = dmul(dsub(tx, le[i]), idds[i]);
+            const long long tb = dbits(ty);
+            if (tb > 0 && tb < 0x41d0000000000000LL) {
+                // 0 < ty < 2^30: floor and fraction from the bits; yt's
+                // clamp of (dims-1, dims) to dims-1 for negative steps does
+                // not change the floor, and the sample position uses the
+                // unclamped coordinate (its sampler recomputes dp from the
+                // ray, image_samplers.pyx:475-478)
+                split_floor(tb, w.cur[i], w.P[i]);
+            } else {
+                double tc = ty;
+                if (-1 < ty && ty < 0 && r.step[i] > 0) tc = 0.0;
+                else if (dims - 1 < ty && ty < dims && r.step[i] < 0) tc = (double)(dims - 1);
+                w.cur[i] = (int)floor(tc);
+                w.P[i] = (float)dsub(ty, (double)w.cur[i]);
+            }
         }
-        if (r.step[i] > 0) ty = dadd(dmul((double)(w.cur[i] + 1), b.dds[i]), b.le[i]);
-        else if (r.step[i] < 0) ty = dadd(dmul((double)w.cur[i], b.dds[i]), b.le[i]);
-        w.tmax[i] = r.step[i] != 0 ? dmul(dsub(ty, r.pos[i]), r.iv[i]) : 1e60;
+        if (r.step[i] != 0) {
+            // (cur+1)*dds + le or cur*dds + le (:105-108), from the table
+            const int k = r.step[i] > 0 ? w.cur[i] + 1 : w.cur[i];
+            const double bv = (k >= 0 && k <= dims) ? ldg(bounds + boff + aoff + k)
+                                                    : dadd(dmul((double)k, ldg(&bp->dds[i])), le[i]);
+            w.tmax[i] = dmul(dsub(bv, r.pos[i]), r.iv[i]);
+        } else {
+            w.tmax[i] = 1e60;
+        }
+        aoff += dims + 1;
     }
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        if (w.cur[i] == b.dims[i] && r.step[i] >= 0) return false;
+        if (w.cur[i] == bf.dims[i] && r.step[i] >= 0) return false;
         if (w.cur[i] == -1 && r.step[i] <= -1) return false;
     }
     w.enter_t = intersect_t;
@@ -423,6 +580,7 @@ struct RayState {
     double tdelta[3];            // cached per dds
     long long last_dds[3];
     double max_t;
+    float max_tf;
     long long kmax;
     bool comp;
 };
@@ -432,6 +590,7 @@ YTGB_HD void ray_state_init(RayState &s, const double *img, double zbuf, bool ha
     max_t = max_t > 0.0 ? max_t : 0.0;  // fclip(z, 0, 1) (image_samplers.pyx:185)
     max_t = max_t < 1.0 ? max_t : 1.0;  // also grid_traversal.pyx:42
     s.max_t = max_t;
+    s.max_tf = (float)max_t;
     s.kmax = dkey(max_t);
     YTGB_UNROLL
     for (int c = 0; c < 4; c++) {
@@ -451,44 +610,238 @@ YTGB_HD void ray_state_init(RayState &s, const double *img, double zbuf, bool ha
     s.comp = !(flags & YTGB_FLAG_NO_COMPENSATION);
 }
 
+// The sampler callback for one visited cell: VolumeRenderSampler.sample
+// (image_samplers.pyx:453-487), ProjectionSampler.sample (:330-343),
+// InterpolatedProjectionSampler.sample (:372-403), the MIP sampler, or the
+// traversal trace.  P is the cell-local entry point, vel the cell-local
+// velocity, dtf = exit_t - enter_t.
+struct CellCtx {
+    const float *base;
+    long long fstride, moff;
+    int nf, sx, sy;
+    int dims[3];
+    float vel[3];
+};
+
+template <int MODE, int CTF>
+YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi, const CellCtx &c, const int cur[3],
+                         const float P[3], float dtf, long long enter_bits, long long exit_bits, RayState &st) {
+    st.visits++;
+    if (MODE == MODE_TRACE) {
+        st.th = fnv_mix(st.th, (unsigned long long)(unsigned)bi);
+        st.th = fnv_mix(st.th, (unsigned long long)(unsigned)cur[0] | ((unsigned long long)(unsigned)cur[1] << 32));
+        st.th = fnv_mix(st.th, (unsigned long long)(unsigned)cur[2]);
+        st.th = fnv_mix(st.th, (unsigned long long)enter_bits);
+        st.th = fnv_mix(st.th, (unsigned long long)exit_bits);
+        st.tcount++;
+        return;
+    }
+    const bool inside = (unsigned)cur[0] < (unsigned)c.dims[0] && (unsigned)cur[1] < (unsigned)c.dims[1] &&
+                        (unsigned)cur[2] < (unsigned)c.dims[2];
+    if (!inside) {
+        // yt hands its sampler this index and reads outside the brick; here
+        // the cell contributes nothing and is counted
+        st.guarded++;
+        return;
+    }
+    float *xh = st.xh, *xl = st.xl;
+    const bool comp = st.comp;
+    if (MODE == MODE_PROJ || MODE == MODE_MIP) {
+        const int di = (cur[0] * c.dims[1] + cur[1]) * c.dims[2] + cur[2];
+        const int nch = c.nf < 4 ? c.nf : 4;
+        YTGB_UNROLL
+        for (int ch = 0; ch < 4; ch++) {
+            if (ch < nch) {
+                const float val = ldg(c.base + ch * c.fstride + di);
+                if (MODE == MODE_PROJ) {
+                    const float inc = fmul(val, dtf);
+                    if (comp) acc_add(xh[ch], xl[ch], inc);
+                    else xh[ch] = fadd(xh[ch], inc);
+                } else if (val > xh[ch]) {
+                    xh[ch] = val;
+                    xl[ch] = 0.0f;
+                }
+                st.touched |= 1u << ch;
+            }
+        }
+        return;
+    }
+    const int cell = (cur[0] * c.dims[1] + cur[1]) * c.dims[2] + cur[2];
+    if (MODE == MODE_VR && c.moff >= 0 && a.masks && ldg(a.masks + c.moff + cell) != 1) return;
+    const int off = cur[0] * c.sx + cur[1] * c.sy + cur[2];
+    const int ns = a.n_samples;
+    const float dts = ns == 1 ? dtf : fdiv(dtf, (float)ns);
+    for (int s = 0; s < ns; s++) {
+        // sample s at enter_t + (s + 1/2) dt (image_samplers.pyx:475-487)
+        const float f = fmul(dts, (float)s + 0.5f);
+        const float fx = fminf(fmaxf(ffma(f, c.vel[0], P[0]), 0.0f), 1.0f);
+        const float fy = fminf(fmaxf(ffma(f, c.vel[1], P[1]), 0.0f), 1.0f);
+        const float fz = fminf(fmaxf(ffma(f, c.vel[2], P[2]), 0.0f), 1.0f);
+        if (MODE == MODE_VR && CTF) {
+            const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
+            const ytgb_tf &tf = a.tf;
+            // outside the table's range: zero emission and absorption leave x
+            // unchanged
+            if (!(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val)) {
+                float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
+                q = fminf(fmaxf(q, 0.0f), (float)(tf.nbins[0] - 2));
+                const int bin = (int)q;
+                const float4 Y = s_tab[3 * bin + 0], D = s_tab[3 * bin + 1];
+                const float4 Z = s_tab[3 * bin + 2];
+                const float dd = fsub(fsub(val, Z.x), Z.y);
+                const float al = ffma(dd, D.w, Y.w);
+                const float er = fmul(ffma(dd, D.x, Y.x), al);
+                const float eg = fmul(ffma(dd, D.y, Y.y), al);
+                const float eb = fmul(ffma(dd, D.z, Y.z), al);
+                if (tf.grey_opacity == 1) {
+                    const float da = fmul(dts, al);
+                    acc_grey(xh[0], xl[0], dts, er, da, comp);
+                    acc_grey(xh[1], xl[1], dts, eg, da, comp);
+                    acc_grey(xh[2], xl[2], dts, eb, da, comp);
+                    acc_grey(xh[3], xl[3], dts, al, da, comp);
+                } else {
+                    acc_emit(xh[0], xl[0], fmul(dts, er), comp);
+                    acc_emit(xh[1], xl[1], fmul(dts, eg), comp);
+                    acc_emit(xh[2], xl[2], fmul(dts, eb), comp);
+                }
+            }
+            st.touched |= a.tf.grey_opacity == 1 ? 0xfu : 0x7u;
+        } else {
+            float dvs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            YTGB_UNROLL
+            for (int fi = 0; fi < 6; fi++)
+                if (fi < c.nf) dvs[fi] = trilinear(c.base + fi * c.fstride + off, c.sy, c.sx, fx, fy, fz);
+            if (MODE == MODE_VR) {
+                float trgba[6];
+                tf_eval(a.tf, s_tab, dvs, trgba);
+                if (a.tf.grey_opacity == 1) {
+                    const float da = fmul(dts, trgba[3]);
+                    YTGB_UNROLL
+                    for (int ch = 0; ch < 4; ch++) acc_grey(xh[ch], xl[ch], dts, trgba[ch], da, comp);
+                    st.touched |= 0xfu;
+                } else {
+                    YTGB_UNROLL
+                    for (int ch = 0; ch < 3; ch++) acc_emit(xh[ch], xl[ch], fmul(dts, trgba[ch]), comp);
+                    st.touched |= 0x7u;
+                }
+            } else {
+                const int n3 = c.nf < 3 ? c.nf : 3;
+                YTGB_UNROLL
+                for (int ch = 0; ch < 3; ch++) {
+                    if (ch < n3) {
+                        const float inc = fmul(dvs[ch], dts);
+                        if (comp) acc_add(xh[ch], xl[ch], inc);
+                        else xh[ch] = fadd(xh[ch], inc);
+                        st.touched |= 1u << ch;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// The float32 geometry of one step: move P to the exit point, then put the
+// stepped axis exactly on the next cell's entry face.
+YTGB_HD void advance_position(float P[3], const float vel[3], float dtf, int i, int step_i) {
+    YTGB_UNROLL
+    for (int q = 0; q < 3; q++) P[q] = ffma(dtf, vel[q], P[q]);
+    const float wrap = step_i > 0 ? 0.0f : 1.0f;
+    if (i == 0) P[0] = wrap;
+    else if (i == 1) P[1] = wrap;
+    else P[2] = wrap;
+}
+
 // One brick of one ray: cast_through_kdtree's walk_volume call
 // (image_samplers.pyx:186) with the sampler callback inlined.
-// s_tab: the transfer-function table as laid out in shared memory (see the
-// kernel prologue); bi: the brick index.
+// s_tab: the transfer-function table as staged in shared memory; bi: the
+// brick index.
 template <int MODE, int CTF>
 YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, int bi, RayState &st) {
     const ytgb_brick *bp = a.bricks + bi;
-    BrickGeom g;
-    load_brick(bp, g);
+    BrickF bf;
+    load_brick_f(bp, bf);
+    if (surely_misses(bf, r, st.max_tf)) return;
     const double max_t = st.max_t;
     const long long kmax = st.kmax;
-    if (surely_misses(g, r, (float)max_t)) return;
     Walk w;
-    if (!walk_setup(g, r, max_t, w)) return;
+    if (!walk_setup(bf, bp, a.bounds, r, max_t, kmax, w)) return;
     // tdelta depends on the ray and dds only (grid_traversal.pyx:86)
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
-        const long long db = dbits(g.dds[i]);
+        const double dds = ldg(&bp->dds[i]);
+        const long long db = dbits(dds);
         if (db != st.last_dds[i]) {
-            st.tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), g.dds[i]);
+            st.tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), dds);
             st.last_dds[i] = db;
         }
     }
     st.walks++;
-    const int nf = ldg(&bp->n_fields);
-    const float *base_p = a.data + ldg(&bp->data_offset);
-    const long long fstride = ldg(&bp->field_stride);
-    const long long moff = ldg(&bp->mask_offset);
-    const int sy = g.dims[2] + 1, sx = (g.dims[1] + 1) * (g.dims[2] + 1);
-    const int step_limit = g.dims[0] + g.dims[1] + g.dims[2] + 3;
-    float vel[3];  // cells per unit t, for the float32 geometry
+    CellCtx c;
+    c.nf = ldg(&bp->n_fields);
+    c.base = a.data + ldg(&bp->data_offset);
+    c.fstride = ldg(&bp->field_stride);
+    c.moff = ldg(&bp->mask_offset);
     YTGB_UNROLL
-    for (int i = 0; i < 3; i++) vel[i] = fmul(r.fdir[i], (float)g.idds[i]);
+    for (int i = 0; i < 3; i++) {
+        c.dims[i] = bf.dims[i];
+        c.vel[i] = fmul(r.fdir[i], bf.iddsf[i]);
+    }
+    c.sy = bf.dims[2] + 1;
+    c.sx = (bf.dims[1] + 1) * (bf.dims[2] + 1);
+    const int step_limit = bf.dims[0] + bf.dims[1] + bf.dims[2] + 3;
+    int hitc = 0;
+    const long long b0 = dbits(w.tmax[0]), b1 = dbits(w.tmax[1]), b2 = dbits(w.tmax[2]);
+    const long long INF = 0x7ff0000000000000LL;
+    if (b0 > 0 && b1 > 0 && b2 > 0 && b0 < INF && b1 < INF && b2 < INF && kmax > 0) {
+        // ---- integer cell loop (positive walk values: key == bits) -----------
+        AxisStep A0, A1, A2;
+        A0.bits = b0;
+        A1.bits = b1;
+        A2.bits = b2;
+        step_prepare(A0, st.tdelta[0]);
+        step_prepare(A1, st.tdelta[1]);
+        step_prepare(A2, st.tdelta[2]);
+        long long eb = dbits(w.enter_t);
+        while (true) {
+            if (++hitc > step_limit) {
+                set_error(a.error, YTGB_DEVERR_STEP_LIMIT);
+                break;
+            }
+            int i;
+            if (A0.bits < A1.bits) i = A0.bits < A2.bits ? 0 : 2;
+            else i = A1.bits < A2.bits ? 1 : 2;
+            const long long tmb = i == 0 ? A0.bits : (i == 1 ? A1.bits : A2.bits);
+            const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
+            const float dtf = MODE == MODE_TRACE ? 0.0f : diff_to_float(xb, eb);
+            sample_cell<MODE, CTF>(a, s_tab, bi, c, w.cur, w.P, dtf, eb, xb, st);
+            // advance (grid_traversal.pyx:134-138)
+            const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
+            advance_position(w.P, c.vel, dtf, i, si);
+            int ci, di;
+            if (i == 0) {
+                w.cur[0] += si;
+                step_advance(A0, st.tdelta[0]);
+                ci = w.cur[0];
+                di = c.dims[0];
+            } else if (i == 1) {
+                w.cur[1] += si;
+                step_advance(A1, st.tdelta[1]);
+                ci = w.cur[1];
+                di = c.dims[1];
+            } else {
+                w.cur[2] += si;
+                step_advance(A2, st.tdelta[2]);
+                ci = w.cur[2];
+                di = c.dims[2];
+            }
+            eb = tmb;
+            if (ci < 0 || ci >= di || !(tmb < kmax)) break;  // ... or enter_t >= max_t
+        }
+        return;
+    }
+    // ---- general cell loop (a walk value <= 0 or not finite) -----------------
     long long K0 = dkey(w.tmax[0]), K1 = dkey(w.tmax[1]), K2 = dkey(w.tmax[2]);
     double enter_t = w.enter_t;
-    int hitc = 0;
-    float *xh = st.xh, *xl = st.xl;
-    const bool comp = st.comp;
     while (true) {
         if (++hitc > step_limit) {
             set_error(a.error, YTGB_DEVERR_STEP_LIMIT);
@@ -499,140 +852,24 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
         else i = K1 < K2 ? 1 : 2;
         const double tm = i == 0 ? w.tmax[0] : (i == 1 ? w.tmax[1] : w.tmax[2]);
         const long long Ki = i == 0 ? K0 : (i == 1 ? K1 : K2);
-        const double exit_t = Ki < kmax ? tm : max_t;  // fmin(tmax[i], max_t)
-        const bool inside = (unsigned)w.cur[0] < (unsigned)g.dims[0] && (unsigned)w.cur[1] < (unsigned)g.dims[1] &&
-                            (unsigned)w.cur[2] < (unsigned)g.dims[2];
-        float dtf = 0.0f;
-        if (MODE != MODE_TRACE) dtf = (float)dsub(exit_t, enter_t);
-        // ---- sampler callback ------------------------------------------------
-        if (MODE == MODE_TRACE) {
-            st.th = fnv_mix(st.th, (unsigned long long)(unsigned)bi);
-            st.th = fnv_mix(st.th, (unsigned long long)(unsigned)w.cur[0] | ((unsigned long long)(unsigned)w.cur[1] << 32));
-            st.th = fnv_mix(st.th, (unsigned long long)(unsigned)w.cur[2]);
-            st.th = fnv_mix(st.th, (unsigned long long)dbits(enter_t));
-            st.th = fnv_mix(st.th, (unsigned long long)dbits(exit_t));
-            st.tcount++;
-        } else if (!inside) {
-            st.guarded++;
-        } else if (MODE == MODE_PROJ || MODE == MODE_MIP) {
-            // ProjectionSampler.sample (image_samplers.pyx:330-343)
-            const int di = (w.cur[0] * g.dims[1] + w.cur[1]) * g.dims[2] + w.cur[2];
-            const int nch = nf < 4 ? nf : 4;
-            YTGB_UNROLL
-            for (int c = 0; c < 4; c++) {
-                if (c < nch) {
-                    const float val = ldg(base_p + c * fstride + di);
-                    if (MODE == MODE_PROJ) {
-                        const float inc = fmul(val, dtf);
-                        if (comp) acc_add(xh[c], xl[c], inc);
-                        else xh[c] = fadd(xh[c], inc);
-                    } else if (val > xh[c]) {
-                        xh[c] = val;
-                        xl[c] = 0.0f;
-                    }
-                    st.touched |= 1u << c;
-                }
-            }
-        } else {
-            // VolumeRenderSampler.sample (image_samplers.pyx:453-487) and
-            // InterpolatedProjectionSampler.sample (:372-403)
-            const int cell = (w.cur[0] * g.dims[1] + w.cur[1]) * g.dims[2] + w.cur[2];
-            bool masked = false;
-            if (MODE == MODE_VR && moff >= 0 && a.masks) masked = ldg(a.masks + moff + cell) != 1;
-            if (!masked) {
-                const int off = w.cur[0] * sx + w.cur[1] * sy + w.cur[2];
-                const int ns = a.n_samples;
-                const float dts = ns == 1 ? dtf : fdiv(dtf, (float)ns);
-                for (int s = 0; s < ns; s++) {
-                    // sample s at enter_t + (s + 1/2) dt (image_samplers.pyx:475-487)
-                    const float f = fmul(dts, (float)s + 0.5f);
-                    const float fx = fminf(fmaxf(ffma(f, vel[0], w.P[0]), 0.0f), 1.0f);
-                    const float fy = fminf(fmaxf(ffma(f, vel[1], w.P[1]), 0.0f), 1.0f);
-                    const float fz = fminf(fmaxf(ffma(f, vel[2], w.P[2]), 0.0f), 1.0f);
-                    if (MODE == MODE_VR && CTF) {
-                        const float val = trilinear(base_p + off, sy, sx, fx, fy, fz);
-                        const ytgb_tf &tf = a.tf;
-                        // out of the table's range: zero emission and
-                        // absorption leave x unchanged
-                        if (!(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val)) {
-                            float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
-                            q = fminf(fmaxf(q, 0.0f), (float)(tf.nbins[0] - 2));
-                            const int bin = (int)q;
-                            const float4 Y = s_tab[3 * bin + 0], D = s_tab[3 * bin + 1];
-                            const float4 Z = s_tab[3 * bin + 2];
-                            const float dd = fsub(fsub(val, Z.x), Z.y);
-                            const float al = ffma(dd, D.w, Y.w);
-                            const float er = fmul(ffma(dd, D.x, Y.x), al);
-                            const float eg = fmul(ffma(dd, D.y, Y.y), al);
-                            const float eb = fmul(ffma(dd, D.z, Y.z), al);
-                            if (tf.grey_opacity == 1) {
-                                const float da = fmul(dts, al);
-                                acc_grey(xh[0], xl[0], dts, er, da, comp);
-                                acc_grey(xh[1], xl[1], dts, eg, da, comp);
-                                acc_grey(xh[2], xl[2], dts, eb, da, comp);
-                                acc_grey(xh[3], xl[3], dts, al, da, comp);
-                            } else {
-                                acc_emit(xh[0], xl[0], fmul(dts, er), comp);
-                                acc_emit(xh[1], xl[1], fmul(dts, eg), comp);
-                                acc_emit(xh[2], xl[2], fmul(dts, eb), comp);
-                            }
-                        }
-                        st.touched |= a.tf.grey_opacity == 1 ? 0xfu : 0x7u;
-                    } else {
-                        float dvs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                        YTGB_UNROLL
-                        for (int fi = 0; fi < 6; fi++)
-                            if (fi < nf) dvs[fi] = trilinear(base_p + fi * fstride + off, sy, sx, fx, fy, fz);
-                        if (MODE == MODE_VR) {
-                            float trgba[6];
-                            tf_eval(a.tf, s_tab, dvs, trgba);
-                            if (a.tf.grey_opacity == 1) {
-                                const float da = fmul(dts, trgba[3]);
-                                YTGB_UNROLL
-                                for (int c = 0; c < 4; c++) acc_grey(xh[c], xl[c], dts, trgba[c], da, comp);
-                                st.touched |= 0xfu;
-                            } else {
-                                YTGB_UNROLL
-                                for (int c = 0; c < 3; c++) acc_emit(xh[c], xl[c], fmul(dts, trgba[c]), comp);
-                                st.touched |= 0x7u;
-                            }
-                        } else {
-                            const int n3 = nf < 3 ? nf : 3;
-                            YTGB_UNROLL
-                            for (int c = 0; c < 3; c++) {
-                                if (c < n3) {
-                                    const float inc = fmul(dvs[c], dts);
-                                    if (comp) acc_add(xh[c], xl[c], inc);
-                                    else xh[c] = fadd(xh[c], inc);
-                                    st.touched |= 1u << c;
-                                }
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        st.visits++;
-        // ---- advance (grid_traversal.pyx:134-138) -----------------------------
-        // float32 geometry: move to the exit point, then put the stepped axis
-        // exactly on the next cell's entry face
-        YTGB_UNROLL
-        for (int q = 0; q < 3; q++) w.P[q] = ffma(dtf, vel[q], w.P[q]);
+        const double exit_t = Ki < kmax ? tm : max_t;
+        const float dtf = MODE == MODE_TRACE ? 0.0f : (float)dsub(exit_t, enter_t);
+        sample_cell<MODE, CTF>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
         const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
-        const float wrap = si > 0 ? 0.0f : 1.0f;
+        advance_position(w.P, c.vel, dtf, i, si);
         const double td = i == 0 ? st.tdelta[0] : (i == 1 ? st.tdelta[1] : st.tdelta[2]);
         const double tn = dadd(tm, td);
         const long long Kn = dkey(tn);
         int ci, di;
         if (i == 0) {
-            w.P[0] = wrap; w.cur[0] += si; w.tmax[0] = tn; K0 = Kn; ci = w.cur[0]; di = g.dims[0];
+            w.cur[0] += si; w.tmax[0] = tn; K0 = Kn; ci = w.cur[0]; di = c.dims[0];
         } else if (i == 1) {
-            w.P[1] = wrap; w.cur[1] += si; w.tmax[1] = tn; K1 = Kn; ci = w.cur[1]; di = g.dims[1];
+            w.cur[1] += si; w.tmax[1] = tn; K1 = Kn; ci = w.cur[1]; di = c.dims[1];
         } else {
-            w.P[2] = wrap; w.cur[2] += si; w.tmax[2] = tn; K2 = Kn; ci = w.cur[2]; di = g.dims[2];
+            w.cur[2] += si; w.tmax[2] = tn; K2 = Kn; ci = w.cur[2]; di = c.dims[2];
         }
         enter_t = tm;
-        if (ci < 0 || ci >= di || !(Ki < kmax)) break;  // ... or enter_t >= max_t
+        if (ci < 0 || ci >= di || !(Ki < kmax)) break;
     }
 }
 

@@ -257,6 +257,20 @@ int check_args(const ytgb_render_args *a, bool trace) {
         ytgb_set_error("ytgb_render: n_samples must be >= 1");
         return YTGB_ERR_INVALID;
     }
+    // the kernels load these with vector / 8-byte accesses
+    auto misaligned = [](const void *p, uintptr_t al) { return p && ((uintptr_t)p & (al - 1)) != 0; };
+    if (misaligned(a->rects, 16) || misaligned(a->tf_tables, 16) || misaligned(a->bricks, 16) ||
+        misaligned(a->bounds, 8) || misaligned(a->image, 8) || misaligned(a->zbuffer, 8) ||
+        misaligned(a->counters, 8) || misaligned(v.px_pos, 8) || misaligned(v.px_dir, 8) ||
+        misaligned(a->order, 4) || misaligned(a->data, 4) || misaligned(a->error, 4)) {
+        ytgb_set_error("ytgb_render: misaligned pointer (rects, tf_tables and bricks need 16 bytes, "
+                       "float64 arrays 8)");
+        return YTGB_ERR_INVALID;
+    }
+    if (a->n_order > 0 && !a->bounds) {
+        ytgb_set_error("ytgb_render: missing cell-boundary tables");
+        return YTGB_ERR_INVALID;
+    }
     if (!trace && a->kind == YTGB_VOLUME_RENDER && !a->tf_tables) {
         ytgb_set_error("ytgb_render: volume rendering needs a transfer function");
         return YTGB_ERR_INVALID;
@@ -444,7 +458,8 @@ extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, i
                                  int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                                  int32_t blocks, void *stream) {
     if (!d_entries || n <= 0 || total_tiles <= 0 || !d_queue || tile_shape < 0 || tile_shape > 2 || kind < 0 ||
-        kind > 3 || smem_bytes < 0 || smem_bytes > 200 * 1024) {
+        kind > 3 || smem_bytes < 0 || smem_bytes > 200 * 1024 || ((uintptr_t)d_entries & 15) != 0 ||
+        ((uintptr_t)d_queue & 3) != 0) {
         ytgb_set_error("ytgb_batch_render: bad arguments");
         return YTGB_ERR_INVALID;
     }

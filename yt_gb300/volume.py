@@ -68,13 +68,21 @@ class BrickSet:
             if mask is not None and not bool(np.all(np.asarray(mask) == 1)):
                 need_mask = True
             mtotal += int(np.prod([int(x) for x in dims]))
+        # cell-boundary tables: for each brick and axis, k*dds + le for
+        # k = 0..dims (the float64 values walk_volume forms for tmax,
+        # grid_traversal.pyx:106-108); numpy's elementwise multiply and add
+        # round exactly like the reference's C expression
+        nb_total = sum(sum(int(x) + 1 for x in b[4]) for b in bricks)
+        bounds = np.empty(max(nb_total, 1), dtype=np.float64)
         buf = _pinned((max(total, 4),), torch.float32, self.device)
         bnp = buf.numpy()
         mbuf = _pinned((max(mtotal, 1),), torch.uint8, self.device) if need_mask else None
+        boff = 0
         for k, (data, mask, le, re, dims) in enumerate(bricks):
             off, stride, moff = offs[k]
             b = self.host[k]
             dims = [int(x) for x in dims]
+            b.bounds_offset = boff
             for i in range(3):
                 b.left_edge[i] = float(le[i])
                 b.right_edge[i] = float(re[i])
@@ -82,6 +90,12 @@ class BrickSet:
                 # PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55)
                 b.dds[i] = (b.right_edge[i] - b.left_edge[i]) / dims[i]
                 b.idds[i] = 1.0 / b.dds[i]
+                b.snap[i] = 1e-10 * b.dds[i]
+                b.lef[i] = b.left_edge[i]
+                b.ref[i] = b.right_edge[i]
+                b.iddsf[i] = b.idds[i]
+                bounds[boff: boff + dims[i] + 1] = np.arange(dims[i] + 1, dtype=np.float64) * b.dds[i] + b.left_edge[i]
+                boff += dims[i] + 1
             b.n_fields = len(data)
             b.data_offset = off
             b.field_stride = stride
@@ -96,6 +110,7 @@ class BrickSet:
             else:
                 b.mask_offset = -1
         self.data = buf.to(self.device, non_blocking=True)
+        self.bounds = torch.from_numpy(bounds).to(self.device)
         self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
         raw = np.frombuffer(self.host, dtype=np.uint8, count=C.sizeof(_lib.Brick) * max(n, 1)).copy()
         self.desc = torch.from_numpy(raw).to(self.device)
@@ -177,6 +192,7 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
     args.order = tab_d.data_ptr() + 4 * 4 * order.size
     args.data = bricks.data.data_ptr()
     args.masks = _ptr(bricks.masks)
+    args.bounds = bricks.bounds.data_ptr()
     if tf is not None:
         args.tf = tf.header
         args.tf_tables = tf.device_tables(dev).data_ptr()
@@ -215,6 +231,7 @@ def trace(bricks: BrickSet, view: _lib.View, order: np.ndarray, zbuffer=None, px
     args.rects = tab_d.data_ptr()
     args.order = tab_d.data_ptr() + 16 * order.size
     args.data = bricks.data.data_ptr()
+    args.bounds = bricks.bounds.data_ptr()
     args.zbuffer = _ptr(zbuffer)
     stream = torch.cuda.current_stream(dev)
     st = _lib.lib().ytgb_trace(C.byref(args), hashes.data_ptr(), counts.data_ptr(), C.c_void_p(stream.cuda_stream))
