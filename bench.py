@@ -332,8 +332,8 @@ def run_ours(args):
             t1 = time.perf_counter()
             if i >= args.warmup:
                 ets.append(t1 - t0)
-        h2d = r.bricks.nbytes + img_h.nbytes + nx * ny * 8 + (ppos.nbytes + pdir.nbytes if ppos is not None else 0)
-        d2h = img_h.nbytes
+        h2d = s.last_h2d_bytes
+        d2h = s.last_d2h_bytes
         e2e_v = samples_step / float(np.median(ets)) / 1e9
         e2e = {"value": e2e_v, "unit": "Gsamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1e3 * float(np.median(ets)), "path": "VolumeRenderSampler(...)(pg) per brick, aimage"}

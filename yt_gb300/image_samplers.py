@@ -122,6 +122,8 @@ class ImageSampler:
         self._pending = []
         self.n_samples = 1
         self.last_counters = None
+        self.last_h2d_bytes = 0
+        self.last_d2h_bytes = 0
 
     # ---- the call surface ---------------------------------------------------
     def __call__(self, pg, **kwa):
@@ -174,6 +176,9 @@ class ImageSampler:
         if self._px_pos is not None:
             px_pos = torch.from_numpy(self._px_pos).to(dev)
             px_dir = torch.from_numpy(self._px_dir).to(dev)
+        h2d = bricks.upload_bytes + img.nbytes + self.azbuffer.size * 8
+        if px_pos is not None:
+            h2d += 2 * self._px_pos.nbytes
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)
         _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb,
@@ -184,6 +189,10 @@ class ImageSampler:
         out = image_d.cpu().numpy()
         self._image[...] = out
         self.last_counters = counters.cpu().numpy()
+        # bytes copied host -> device (bricks, boundary tables, descriptors,
+        # image, zbuffer, per-pixel rays, order and rectangles) and back
+        self.last_h2d_bytes = int(h2d + 20 * len(pending))
+        self.last_d2h_bytes = int(out.nbytes + 4 * 8)
 
     def ensure_code_unit_params(self, params):
         for name in ["center", "vp_pos", "vp_dir", "width"]:

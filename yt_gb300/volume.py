@@ -31,6 +31,18 @@ def _pinned(shape, dtype, device) -> torch.Tensor:
     return t
 
 
+# numpy view of ytgb_brick (include/ytgb.h), field for field
+BRICK_DTYPE = np.dtype({
+    "names": ["left_edge", "right_edge", "dds", "idds", "snap", "dims", "n_fields", "data_offset", "field_stride",
+              "mask_offset", "bounds_offset", "lef", "ref", "iddsf", "pad"],
+    "formats": [("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<i4", 3), "<i4", "<i8", "<i8", "<i8",
+                "<i8", ("<f4", 3), ("<f4", 3), ("<f4", 3), ("<i4", 5)],
+    "offsets": [0, 24, 48, 72, 96, 120, 132, 136, 144, 152, 160, 168, 180, 192, 204],
+    "itemsize": 224,
+})
+assert BRICK_DTYPE.itemsize == C.sizeof(_lib.Brick)
+
+
 class BrickSet:
     """Bricks ``(data, mask, left_edge, right_edge, dims)`` resident on ``device``.
 
@@ -42,79 +54,92 @@ class BrickSet:
         self.device = torch.device(device)
         n = len(bricks)
         self.n = n
-        self.host = (_lib.Brick * max(n, 1))()
-        offs = []
-        total = 0
-        mtotal = 0
+        m = max(n, 1)
+        desc = np.zeros(m, dtype=BRICK_DTYPE)
+        dims = np.ones((m, 3), dtype=np.int64)
+        le = np.zeros((m, 3))
+        re = np.ones((m, 3))
+        nfields = np.zeros(m, dtype=np.int64)
+        sizes = []
         need_mask = False
-        self.min_elems = np.zeros(max(n, 1), dtype=np.int64)
-        self.cells = np.zeros(max(n, 1), dtype=np.int64)
-        self.verts = np.zeros(max(n, 1), dtype=np.int64)
-        for k, (data, mask, _le, _re, dims) in enumerate(bricks):
-            dims_i = [int(x) for x in dims]
-            if len(dims_i) != 3 or min(dims_i) <= 0:
-                raise ValueError(f"brick {k}: dims must be 3 positive integers, got {dims_i}")
+        for k, (data, mask, le_k, re_k, dims_k) in enumerate(bricks):
+            d3 = [int(x) for x in dims_k]
+            if len(d3) != 3 or min(d3) <= 0:
+                raise ValueError(f"brick {k}: dims must be 3 positive integers, got {d3}")
             if not 1 <= len(data) <= 6:
                 raise ValueError(f"brick {k}: 1 to 6 fields supported, got {len(data)}")
-            if mask is not None and int(np.asarray(mask).size) != int(np.prod(dims_i)):
-                raise ValueError(f"brick {k}: mask must have prod(dims) entries")
-            sizes = [int(np.asarray(d).size) for d in data]
-            self.min_elems[k] = min(sizes)
-            self.cells[k] = int(np.prod(dims_i))
-            self.verts[k] = int(np.prod([d + 1 for d in dims_i]))
-            stride = _align4(max(sizes) if sizes else 0)
-            offs.append((total, stride, mtotal))
-            total += stride * len(data)
-            if mask is not None and not bool(np.all(np.asarray(mask) == 1)):
-                need_mask = True
-            mtotal += int(np.prod([int(x) for x in dims]))
+            if mask is not None:
+                mk = np.asarray(mask)
+                if int(mk.size) != d3[0] * d3[1] * d3[2]:
+                    raise ValueError(f"brick {k}: mask must have prod(dims) entries")
+                if not need_mask and not bool(np.all(mk == 1)):
+                    need_mask = True
+            dims[k] = d3
+            le[k] = le_k[:3]
+            re[k] = re_k[:3]
+            nfields[k] = len(data)
+            sizes.append([int(np.asarray(d).size) for d in data])
+        self.cells = dims.prod(axis=1)
+        self.verts = (dims + 1).prod(axis=1)
+        self.min_elems = np.array([min(sz) for sz in sizes] + [0] * (m - n), dtype=np.int64)
+        stride = np.array([_align4(max(sz)) for sz in sizes] + [0] * (m - n), dtype=np.int64)
+        data_off = np.concatenate([[0], np.cumsum(stride * nfields)])[:m]
+        total = int((stride * nfields).sum())
+        # PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55), elementwise
+        dds = (re - le) / dims
+        idds = 1.0 / dds
+        desc["left_edge"] = le
+        desc["right_edge"] = re
+        desc["dds"] = dds
+        desc["idds"] = idds
+        desc["snap"] = 1e-10 * dds
+        desc["dims"] = dims
+        desc["n_fields"] = nfields
+        desc["data_offset"] = data_off
+        desc["field_stride"] = stride
+        desc["lef"] = le.astype(np.float32)
+        desc["ref"] = re.astype(np.float32)
+        desc["iddsf"] = idds.astype(np.float32)
         # cell-boundary tables: for each brick and axis, k*dds + le for
         # k = 0..dims (the float64 values walk_volume forms for tmax,
         # grid_traversal.pyx:106-108); numpy's elementwise multiply and add
         # round exactly like the reference's C expression
-        nb_total = sum(sum(int(x) + 1 for x in b[4]) for b in bricks)
-        bounds = np.empty(max(nb_total, 1), dtype=np.float64)
+        cnt = (dims + 1)[:n].ravel()
+        starts = np.concatenate([[0], np.cumsum(cnt)])
+        nb_total = int(starts[-1])
+        kk = np.arange(nb_total, dtype=np.float64) - np.repeat(starts[:-1], cnt)
+        bounds = kk * np.repeat(dds[:n].ravel(), cnt) + np.repeat(le[:n].ravel(), cnt)
+        desc["bounds_offset"][:n] = starts[:-1].reshape(n, 3)[:, 0] if n else []
+        if nb_total == 0:
+            bounds = np.zeros(1)
         buf = _pinned((max(total, 4),), torch.float32, self.device)
         bnp = buf.numpy()
+        mtotal = int(self.cells[:n].sum()) if n else 0
         mbuf = _pinned((max(mtotal, 1),), torch.uint8, self.device) if need_mask else None
-        boff = 0
-        for k, (data, mask, le, re, dims) in enumerate(bricks):
-            off, stride, moff = offs[k]
-            b = self.host[k]
-            dims = [int(x) for x in dims]
-            b.bounds_offset = boff
-            for i in range(3):
-                b.left_edge[i] = float(le[i])
-                b.right_edge[i] = float(re[i])
-                b.dims[i] = dims[i]
-                # PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55)
-                b.dds[i] = (b.right_edge[i] - b.left_edge[i]) / dims[i]
-                b.idds[i] = 1.0 / b.dds[i]
-                b.snap[i] = 1e-10 * b.dds[i]
-                b.lef[i] = b.left_edge[i]
-                b.ref[i] = b.right_edge[i]
-                b.iddsf[i] = b.idds[i]
-                bounds[boff: boff + dims[i] + 1] = np.arange(dims[i] + 1, dtype=np.float64) * b.dds[i] + b.left_edge[i]
-                boff += dims[i] + 1
-            b.n_fields = len(data)
-            b.data_offset = off
-            b.field_stride = stride
-            for f, d in enumerate(data):
+        # float64 -> float32 copies into the pinned arena
+        for k in range(n):
+            off, st = int(data_off[k]), int(stride[k])
+            for f, d in enumerate(bricks[k][0]):
                 a = np.asarray(d).ravel()
-                bnp[off + f * stride: off + f * stride + a.size] = a
+                bnp[off + f * st: off + f * st + a.size] = a
+        moff = 0
+        for k, (data, mask, _le, _re, _dims) in enumerate(bricks):
             if need_mask and mask is not None:
-                mnp = mbuf.numpy()
-                m = np.asarray(mask, dtype=np.uint8).ravel()
-                mnp[moff: moff + m.size] = m
-                b.mask_offset = moff
+                mk = np.asarray(mask, dtype=np.uint8).ravel()
+                mbuf.numpy()[moff: moff + mk.size] = mk
+                desc["mask_offset"][k] = moff
             else:
-                b.mask_offset = -1
+                desc["mask_offset"][k] = -1
+            moff += int(self.cells[k])
+        self.desc_host = desc
+        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
         self.data = buf.to(self.device, non_blocking=True)
-        self.bounds = torch.from_numpy(bounds).to(self.device)
         self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
-        raw = np.frombuffer(self.host, dtype=np.uint8, count=C.sizeof(_lib.Brick) * max(n, 1)).copy()
-        self.desc = torch.from_numpy(raw).to(self.device)
+        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
+        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
         self.nbytes = int(self.data.numel() * 4)
+        self.upload_bytes = int(self.data.numel() * 4 + self.bounds.numel() * 8 + self.desc.numel() +
+                                (self.masks.numel() if self.masks is not None else 0))
 
     def rects(self, view: _lib.View, order: np.ndarray) -> np.ndarray:
         """Per-order-entry pixel rectangles (ytgb_brick_rects)."""
