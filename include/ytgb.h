@@ -206,6 +206,24 @@ int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind
                       int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                       int32_t blocks, void *stream);
 
+/* ---- host: brick marshalling -------------------------------------------- */
+/* No reference counterpart: yt's sampler reads each PartitionedGrid's
+ * float64 arrays in place (image_samplers.pyx:146-197, partitioned_grid.pyx:
+ * 38-70).  The device path gathers every brick's fields into one float32
+ * arena per render: dst[dst_offset[k] + i] = (float)src[k][i] for
+ * i < count[k], k < n, on up to n_threads host threads (<= 0: all cores).
+ * Round to nearest even, as numpy's astype(float32). */
+int ytgb_pack_fields(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
+                     float *dst, int32_t n_threads);
+/* The same gather for uint8 cell masks (dst may be NULL: check only);
+ * *all_ones = 1 when every mask byte is 1 (VolumeRenderSampler then needs no
+ * mask, image_samplers.pyx:461-462). */
+int ytgb_pack_masks(const uint8_t *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
+                    uint8_t *dst, int32_t n_threads, int32_t *all_ones);
+/* *result = 1 when all n float64 values have the bit pattern of `value`
+ * (an all-zero image needs no upload; an all-ones zbuffer equals none). */
+int ytgb_host_is_uniform(const double *x, int64_t n, double value, int32_t n_threads, int32_t *result);
+
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
  * amr_kdtools.Node.add_grids / insert_grids / split_grids /

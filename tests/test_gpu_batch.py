@@ -25,6 +25,57 @@ def cams(n, seed=0):
     return out
 
 
+def same_bits(a, b):
+    """Bit-for-bit equality (NaN-safe, unlike torch.equal)."""
+    return a.shape == b.shape and torch.equal(a.view(torch.int64), b.view(torch.int64))
+
+
+def mv_tf(lo, hi):
+    """A general (non-ColorTransferFunction) table set: two tables on field
+    0, the second weighted by field 1 and by table 0."""
+    from yt_gb300.transfer_functions import MultiVariateTransferFunction, TransferFunction
+
+    mv = MultiVariateTransferFunction()
+    t0 = TransferFunction((lo, hi), 64)
+    t0.add_gaussian(0.5 * (lo + hi), 0.05 * (hi - lo), 1.0)
+    t1 = TransferFunction((lo, hi), 200)
+    t1.add_gaussian(0.7 * lo + 0.3 * hi, 0.05 * (hi - lo), 0.8)
+    mv.add_field_table(t0, 0)
+    mv.add_field_table(t1, 0, weight_field_id=1, weight_table_id=0)
+    mv.link_channels(1, [0, 1, 2])
+    return mv
+
+
+@pytest.mark.parametrize("blocks", [0, 1])
+def test_batch_every_sampler_path(cuda, blocks):
+    """Each sampler path of the persistent kernel (colour-table and general
+    volume rendering, projection, interpolated projection, MIP) against
+    render_kernel, with the tiles spread over many blocks or all in one."""
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=0)
+    kd = AMRKDTree(grids, log_field=False)
+    bricks = kd.bricks()
+    # a second, positive field for the weighted table
+    two = [([d[0], np.sqrt(np.abs(d[0]))], m, le, re, dims) for d, m, le, re, dims in bricks]
+    lo = float(min(np.min(d[0]) for d, *_ in bricks))
+    hi = float(max(np.max(d[0]) for d, *_ in bricks))
+    r_mv = Renderer(two, mv_tf(lo, hi), device=cuda, kdtree=kd)
+    r_lin = Renderer(bricks, None, device=cuda, kdtree=kd)
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
+    r_ctf = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
+    cases = [(r_ctf, _lib.VOLUME_RENDER, 1), (r_mv, _lib.VOLUME_RENDER, 2), (r_lin, _lib.PROJECTION, 1),
+             (r_lin, _lib.INTERPOLATED_PROJECTION, 3), (r_lin, _lib.MIP, 1)]
+    jobs = [Job(r, cam, kind, n_samples=ns) for (r, kind, ns) in cases for cam in cams(4, seed=7)]
+    b = Batch(jobs, device=cuda, blocks=blocks)
+    assert len(b.groups) == 5
+    b.launch()
+    torch.cuda.synchronize()
+    b.check()
+    for j in jobs:
+        alone = j.renderer.render(j.camera, kind=j.kind, n_samples=j.n_samples)
+        assert not torch.isnan(alone).any()
+        assert same_bits(alone, j.image), (j.kind, j.n_samples)
+
+
 @pytest.mark.parametrize("tile_shape", [0, 1, 2])
 def test_batch_equals_single_views(cuda, tile_shape):
     w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
@@ -45,14 +96,14 @@ def test_batch_equals_single_views(cuda, tile_shape):
     for j in jobs:
         alone = j.renderer.render(j.camera, kind=j.kind, n_samples=j.n_samples,
                                   flags=tile_shape << _lib.FLAG_TILE_SHIFT)
-        assert torch.equal(alone, j.image)
+        assert same_bits(alone, j.image)
     g = b.capture()
     snap = [im.clone() for im in b.images]
     for _ in range(2):
         g.replay()
     torch.cuda.synchronize()
     for a, s in zip(b.images, snap):
-        assert torch.equal(a, s)
+        assert same_bits(a, s)
     # one view against the oracle
     j = jobs[0]
     p = j.camera.sampler_params()
@@ -71,7 +122,7 @@ def test_batch_projection_and_mip(cuda):
     b.launch()
     torch.cuda.synchronize()
     for j in jobs:
-        assert torch.equal(r.render(j.camera, kind=j.kind), j.image)
+        assert same_bits(r.render(j.camera, kind=j.kind), j.image)
 
 
 def test_batch_rejects_mixed_layouts():

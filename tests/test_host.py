@@ -146,6 +146,25 @@ def test_tf_pack_rejects_bad_input():
         pack(Bad())
 
 
+def test_tf_pack_out_of_float32_range():
+    """Tables whose bounds overflow float32 pack only when all-zero (they
+    evaluate to 0 everywhere, as yt's float64 lookup does)."""
+    from yt_gb300.transfer_functions import MultiVariateTransferFunction, TransferFunction
+
+    def one_table(t):
+        mv = MultiVariateTransferFunction()
+        mv.add_field_table(t, 0)
+        mv.link_channels(0, [0, 1, 2])
+        return mv
+
+    pk = pack(one_table(TransferFunction((-1e60, 1e60), 2)))
+    assert pk.header.hi_excl[0] == -np.inf and pk.header.lo_excl[0] == np.inf
+    nonzero = TransferFunction((-1e60, 1e60), 4)
+    nonzero.y[:] = 1.0
+    with pytest.raises(_lib.YtgbError, match="float32 range"):
+        pack(one_table(nonzero))
+
+
 def test_brick_rects_rejects_bad_order(amr_small):
     w = amr_small
     cam = w.views[0].camera

@@ -174,6 +174,19 @@ def test_grey_opacity_and_multivariate(emu):
     check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=mv)
 
 
+def test_projection_transfer_function_bounds(emu):
+    """ProjectionTransferFunction's +-1e60 bounds have no float32 form; yt's
+    float64 lookup of its all-zero table gives 0 everywhere, and so must the
+    packed table (not NaN)."""
+    from yt_gb300.transfer_functions import ProjectionTransferFunction
+
+    w = workloads.uniform_vr(n=16, res=24)
+    cam = Camera((1.2, 0.3, -0.8), 0.5, 1.0, 24)
+    img, *_ = run_emu(emu, w.bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=ProjectionTransferFunction())
+    assert not np.isnan(img).any()
+    check(emu, w.bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=ProjectionTransferFunction())
+
+
 def test_masked_cells(emu):
     w = workloads.uniform_vr(n=16, res=32)
     data, _, le, re, dims = w.bricks[0]

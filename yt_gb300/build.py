@@ -25,7 +25,7 @@ LIB = OUTDIR / "libytgb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ytgb_render.cu"]
-CPP_SOURCES = ["ytgb_host.cpp"]
+CPP_SOURCES = ["ytgb_host.cpp", "ytgb_pack.cpp"]
 
 
 def _nvcc() -> str:
@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
-    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -2,6 +2,7 @@
 // function packing and the AMR kd-tree.  Compiled with -ffp-contract=off so
 // that its float64 arithmetic rounds exactly like yt's compiled Cython.
 #include <cmath>
+#include <limits>
 #include <cstdint>
 #include <cstring>
 #include <climits>
@@ -221,6 +222,24 @@ extern "C" int ytgb_tf_pack(int32_t n_fits, const double *const *values, const i
         tf->hi_excl[t] = float_at_or_above(b1);
         tf->b0[t] = (float)b0;
         tf->idbin[t] = (float)idbin;
+        // Bounds beyond float32's range (ProjectionTransferFunction uses
+        // +-1e60, transfer_functions.py:946-960) leave no float32 form of the
+        // bin arithmetic.  yt's float64 lookup of such a table returns
+        // values[bin] + (x - d0[bin]) * dy[bin]; when every value is zero that
+        // is 0 for every finite x, which excluding every input reproduces.
+        // Any other table of that kind is rejected.
+        const float fmax = std::numeric_limits<float>::max();
+        if (!(std::fabs(b0) <= fmax && std::fabs(b1) <= fmax) || !(tf->idbin[t] > 0.0f) ||
+            !std::isfinite(tf->idbin[t])) {
+            bool zero = true;
+            for (int b = 0; b < nbins[t]; b++) zero = zero && values[t][b] == 0.0;
+            if (!zero) {
+                ytgb_set_error("ytgb_tf_pack: transfer-function bounds or bin width outside float32 range");
+                return YTGB_ERR_INVALID;
+            }
+            tf->lo_excl[t] = std::numeric_limits<float>::infinity();
+            tf->hi_excl[t] = -std::numeric_limits<float>::infinity();
+        }
         float *tab = tables + (size_t)t * nbmax * 4;
         for (int b = 0; b < nbmax; b++) {
             float y = 0.f, dy = 0.f, d0h = 0.f, d0l = 0.f;

@@ -191,6 +191,20 @@ __global__ void __launch_bounds__(BLOCK) render_kernel(const ytgb_render_args a,
     render_tile<MODE, CTF, TS>(a, blockIdx.y, blockIdx.x, s_tab, sm, hashes, counts);
 }
 
+// The batch kernel renders each work item through this out-of-line copy of
+// render_tile.  With render_tile inlined into the persistent loop, sm_103a
+// builds of the interpolated-projection sampler produced images that differed
+// from render_kernel's under some optimisation settings (-O3, ptxas -O1, the
+// launch arguments staged in shared memory) and not under others; the cause
+// was not identified.  Called out of line, every sampler, tile shape and
+// block count tested matches render_kernel bit for bit.  One call per tile
+// costs nothing measurable.
+template <int MODE, int CTF, int TS>
+__device__ __noinline__ void render_tile_outlined(const ytgb_render_args &a, int bx, int by, float4 *s_tab,
+                                                  TileSmem &sm) {
+    render_tile<MODE, CTF, TS>(a, bx, by, s_tab, sm, nullptr, nullptr);
+}
+
 // Many views in one persistent launch: blocks pull (view, tile) work items
 // from a device counter until the batch is drained, so small and large views
 // share the GPU without a launch per view.  Entries are sorted by
@@ -219,7 +233,7 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(const ytgb_batch_entry *en
         const ytgb_batch_entry &e = entries[lo];
         const int t = item - __ldg(&e.tile_begin);
         const int ty = __ldg(&e.tiles_y);
-        render_tile<MODE, CTF, TS>(e.args, t / ty, t % ty, s_tab, sm, nullptr, nullptr);
+        render_tile_outlined<MODE, CTF, TS>(e.args, t / ty, t % ty, s_tab, sm);
     }
 }
 

@@ -20,10 +20,6 @@ import torch
 from . import _lib
 
 
-def _align4(n: int) -> int:
-    return (n + 3) & ~3
-
-
 def _pinned(shape, dtype, device) -> torch.Tensor:
     t = torch.empty(shape, dtype=dtype)
     if torch.device(device).type == "cuda":
@@ -56,33 +52,57 @@ class BrickSet:
         self.n = n
         m = max(n, 1)
         desc = np.zeros(m, dtype=BRICK_DTYPE)
+        f64 = np.dtype(np.float64)
+        dims_l, le_l, re_l, nf_l = [], [], [], []
+        fields = []     # float64 C-contiguous arrays, all bricks' fields in order
+        masks = []      # (brick, uint8 C-contiguous mask)
+        for k, (data, mask, le_k, re_k, dims_k) in enumerate(bricks):
+            dims_l.append(dims_k)
+            le_l.append(le_k[:3])
+            re_l.append(re_k[:3])
+            nf_l.append(len(data))
+            for d in data:
+                if not (type(d) is np.ndarray and d.dtype == f64 and d.flags.c_contiguous):
+                    d = np.ascontiguousarray(d, dtype=np.float64)
+                fields.append(d)
+            if mask is not None:
+                mk = np.asarray(mask)
+                if mk.dtype == np.bool_:
+                    mk = mk.view(np.uint8)
+                masks.append((k, np.ascontiguousarray(mk, dtype=np.uint8)))
         dims = np.ones((m, 3), dtype=np.int64)
         le = np.zeros((m, 3))
         re = np.ones((m, 3))
         nfields = np.zeros(m, dtype=np.int64)
-        sizes = []
-        need_mask = False
-        for k, (data, mask, le_k, re_k, dims_k) in enumerate(bricks):
-            d3 = [int(x) for x in dims_k]
-            if len(d3) != 3 or min(d3) <= 0:
-                raise ValueError(f"brick {k}: dims must be 3 positive integers, got {d3}")
-            if not 1 <= len(data) <= 6:
-                raise ValueError(f"brick {k}: 1 to 6 fields supported, got {len(data)}")
-            if mask is not None:
-                mk = np.asarray(mask)
-                if int(mk.size) != d3[0] * d3[1] * d3[2]:
-                    raise ValueError(f"brick {k}: mask must have prod(dims) entries")
-                if not need_mask and not bool(np.all(mk == 1)):
-                    need_mask = True
-            dims[k] = d3
-            le[k] = le_k[:3]
-            re[k] = re_k[:3]
-            nfields[k] = len(data)
-            sizes.append([int(np.asarray(d).size) for d in data])
+        if n:
+            try:
+                dims[:n] = np.array(dims_l, dtype=np.int64).reshape(n, 3)
+            except ValueError:
+                raise ValueError("brick dims must be 3 positive integers") from None
+            le[:n] = np.array(le_l, dtype=np.float64)
+            re[:n] = np.array(re_l, dtype=np.float64)
+            nfields[:n] = nf_l
+        bad = np.nonzero((dims[:n] <= 0).any(axis=1) | (nfields[:n] < 1) | (nfields[:n] > 6))[0]
+        if bad.size:
+            k = int(bad[0])
+            raise ValueError(f"brick {k}: dims must be 3 positive integers and 1 to 6 fields are supported "
+                             f"(dims {dims[k].tolist()}, {int(nfields[k])} fields)")
+        if masks:
+            mk_brick = np.array([k for k, _ in masks], dtype=np.int64)
+            mk_size = np.array([mk.size for _, mk in masks], dtype=np.int64)
+            wrong = np.nonzero(mk_size != dims[mk_brick].prod(axis=1))[0]
+            if wrong.size:
+                raise ValueError(f"brick {int(mk_brick[wrong[0]])}: mask must have prod(dims) entries")
+        fsize = np.array([a.size for a in fields], dtype=np.int64)
+        fstart = np.concatenate([[0], np.cumsum(nfields[:n])]).astype(np.int64)
+        sizes_min = np.minimum.reduceat(fsize, fstart[:-1]) if n else fsize
+        sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
         self.cells = dims.prod(axis=1)
         self.verts = (dims + 1).prod(axis=1)
-        self.min_elems = np.array([min(sz) for sz in sizes] + [0] * (m - n), dtype=np.int64)
-        stride = np.array([_align4(max(sz)) for sz in sizes] + [0] * (m - n), dtype=np.int64)
+        self.min_elems = np.zeros(m, dtype=np.int64)
+        self.min_elems[:n] = sizes_min
+        stride = np.zeros(m, dtype=np.int64)
+        stride[:n] = (sizes_max + 3) & ~3
         data_off = np.concatenate([[0], np.cumsum(stride * nfields)])[:m]
         total = int((stride * nfields).sum())
         # PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55), elementwise
@@ -113,24 +133,29 @@ class BrickSet:
         if nb_total == 0:
             bounds = np.zeros(1)
         buf = _pinned((max(total, 4),), torch.float32, self.device)
-        bnp = buf.numpy()
-        mtotal = int(self.cells[:n].sum()) if n else 0
-        mbuf = _pinned((max(mtotal, 1),), torch.uint8, self.device) if need_mask else None
-        # float64 -> float32 copies into the pinned arena
-        for k in range(n):
-            off, st = int(data_off[k]), int(stride[k])
-            for f, d in enumerate(bricks[k][0]):
-                a = np.asarray(d).ravel()
-                bnp[off + f * st: off + f * st + a.size] = a
-        moff = 0
-        for k, (data, mask, _le, _re, _dims) in enumerate(bricks):
-            if need_mask and mask is not None:
-                mk = np.asarray(mask, dtype=np.uint8).ravel()
-                mbuf.numpy()[moff: moff + mk.size] = mk
-                desc["mask_offset"][k] = moff
-            else:
-                desc["mask_offset"][k] = -1
-            moff += int(self.cells[k])
+        L = _lib.lib()
+        # float64 -> float32 gather into the pinned arena, on all host cores
+        src = np.array([a.ctypes.data for a in fields], dtype=np.uintp)
+        fbrick = np.repeat(np.arange(n), nfields[:n])
+        dst_f = (data_off[fbrick] + (np.arange(len(fields)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
+        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fields),
+                                      buf.data_ptr(), 0), "ytgb_pack_fields")
+        # masks: kept only when some cell is masked out
+        mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
+        desc["mask_offset"][:] = -1
+        mbuf = None
+        if masks:
+            msrc = np.array([mk.ctypes.data for _, mk in masks], dtype=np.uintp)
+            mcnt = mk_size
+            mdst = mstart[mk_brick]
+            ones = C.c_int32()
+            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(masks), None, 0,
+                                         C.byref(ones)), "ytgb_pack_masks")
+            if not ones.value:
+                mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
+                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(masks),
+                                             mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
+                desc["mask_offset"][mk_brick] = mdst
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
         self.data = buf.to(self.device, non_blocking=True)
