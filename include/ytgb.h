@@ -206,6 +206,22 @@ int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind
                       int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                       int32_t blocks, void *stream);
 
+/* The same render with nothing allocated by the caller or the call: the
+ * planned host table (h_entries, from ytgb_batch_plan) is copied into a
+ * static device region of this library that also holds the work-queue
+ * counter, then the persistent launch runs from there.  No counterpart in
+ * the reference (yt renders one camera at a time and allocates per call).
+ * Limits: at most YTGB_NOALLOC_MAX_ENTRIES views per call (more is rejected
+ * with YTGB_ERR_INVALID); the region is per device, so calls on one device
+ * must not overlap in time (use one stream, or wait for the previous call's
+ * work); the first call on a device looks the region up
+ * (cudaGetSymbolAddress) -- make it outside any stream capture.  The
+ * counter is cleared by every call; nothing needs to be zero beforehand. */
+#define YTGB_NOALLOC_MAX_ENTRIES 128
+int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+                              int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t blocks,
+                              void *stream);
+
 /* ---- host: brick marshalling -------------------------------------------- */
 /* No reference counterpart: yt's sampler reads each PartitionedGrid's
  * float64 arrays in place (image_samplers.pyx:146-197, partitioned_grid.pyx:

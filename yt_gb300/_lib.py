@@ -19,6 +19,7 @@ LENS_PLANE_PARALLEL, LENS_PER_PIXEL, LENS_PERSPECTIVE = 0, 1, 2
 EXTENT_PLANE_PARALLEL, EXTENT_PERSPECTIVE, EXTENT_NULL = 0, 1, 2
 FLAG_NO_COMPENSATION = 1
 FLAG_TILE_SHIFT = 8
+NOALLOC_MAX_ENTRIES = 128  # YTGB_NOALLOC_MAX_ENTRIES
 FNV_OFFSET = 1469598103934665603
 
 _dp = C.POINTER(C.c_double)
@@ -139,6 +140,8 @@ SIGNATURES = {
                                   C.POINTER(C.c_int32)]),
     "ytgb_batch_render": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                     C.c_void_p, C.c_int32, C.c_void_p]),
+    "ytgb_batch_render_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                            C.c_int32, C.c_int32, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                   C.POINTER(C.c_int32)]),

@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "ytgb.h"
@@ -494,6 +495,108 @@ extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, i
         return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
     default:
         return batch_launch_ts<MODE_MIP, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
+    }
+}
+
+// ---- ytgb_batch_render_noalloc: the persistent batch with static scratch --
+//
+// ytgb_batch_render needs two device buffers from its caller: the planned
+// entry table and the work-queue counter.  Some callers cannot allocate
+// them.  cudaMalloc and cudaFree synchronise the whole device, which a
+// serving loop overlapping renders with other work cannot afford per call;
+// a process whose device memory is already reserved by another allocator
+// (a framework's caching pool) can see a raw cudaMalloc fail; and a caller
+// that holds only host data and pointers it was given (a binding that
+// forwards yt's samplers) has no device allocator to call.  This variant
+// keeps both buffers in a fixed region of static device memory instead, so
+// the call allocates nothing.
+//
+// Layout of the region: the work-queue counter in the first 256 bytes, then
+// up to YTGB_NOALLOC_MAX_ENTRIES entries.  The counter must be zero when the
+// kernel starts; every call clears it on its stream before the launch and
+// overwrites the entries it uses, so nothing has to be zero beforehand.
+// There is one region per device, so calls whose work overlaps on the
+// device (two streams, or two host threads, with launches in flight at the
+// same time) would overwrite each other's table and share one counter:
+// callers must order them (one stream, or wait for one call's work before
+// issuing the next).
+constexpr size_t NOALLOC_QUEUE_BYTES = 256;
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[NOALLOC_QUEUE_BYTES + (size_t)YTGB_NOALLOC_MAX_ENTRIES * sizeof(ytgb_batch_entry)];
+
+namespace {
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// The region's device address, looked up once per device with that device
+// current (the first call on a device does it).
+int noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_batch_render_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        ytgb_set_error("ytgb_batch_render_noalloc: device ordinal out of range");
+        return YTGB_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            ytgb_set_error(std::string("ytgb_batch_render_noalloc: cudaGetSymbolAddress: ") +
+                           cudaGetErrorString(e));
+            return YTGB_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return YTGB_OK;
+}
+}  // namespace
+
+extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind,
+                                         int32_t ctf_fast, int32_t tile_shape, int32_t total_tiles,
+                                         int32_t smem_bytes, int32_t blocks, void *stream) {
+    if (n > YTGB_NOALLOC_MAX_ENTRIES) {
+        ytgb_set_error("ytgb_batch_render_noalloc: " + std::to_string(n) + " entries exceed the static scratch (" +
+                       std::to_string(YTGB_NOALLOC_MAX_ENTRIES) +
+                       " views); split the batch or use ytgb_batch_render with a caller-allocated table");
+        return YTGB_ERR_INVALID;
+    }
+    if (!h_entries || n <= 0 || total_tiles <= 0 || tile_shape < 0 || tile_shape > 2 || kind < 0 || kind > 3 ||
+        smem_bytes < 0 || smem_bytes > 200 * 1024) {
+        ytgb_set_error("ytgb_batch_render_noalloc: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    unsigned char *base = nullptr;
+    if (int st = noalloc_scratch(&base)) return st;
+    int32_t *queue = reinterpret_cast<int32_t *>(base);
+    ytgb_batch_entry *entries = reinterpret_cast<ytgb_batch_entry *>(base + NOALLOC_QUEUE_BYTES);
+    cudaStream_t s = (cudaStream_t)stream;
+    // the host table is consumed before the call returns (a copy from
+    // pageable memory is staged synchronously); the caller may reuse it
+    cudaError_t e = cudaMemcpyAsync(entries, h_entries, (size_t)n * sizeof(ytgb_batch_entry),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_batch_render_noalloc: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    const size_t smem = (size_t)smem_bytes;
+    switch (kind) {
+    case YTGB_VOLUME_RENDER:
+        return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s)
+                        : batch_launch_ts<MODE_VR, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
+    case YTGB_PROJECTION:
+        return batch_launch_ts<MODE_PROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
+    case YTGB_INTERPOLATED_PROJECTION:
+        return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
+    default:
+        return batch_launch_ts<MODE_MIP, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
     }
 }
 
