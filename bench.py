@@ -248,14 +248,18 @@ def run_ours(args):
     image = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
     stream = torch.cuda.current_stream(dev)
+    from yt_gb300.autotune import tile_shape_for
     from yt_gb300.volume import render as vrender
 
+    tile_shape = args.tile_shape if args.tile_shape >= 0 else tile_shape_for(
+        _lib.VOLUME_RENDER, bool(r.packed.header.ctf_fast), view.lens)
+    tflags = tile_shape << _lib.FLAG_TILE_SHIFT
     keep = []
 
     def step():
         image.zero_()
         vrender(r.bricks, view, order, _lib.VOLUME_RENDER, image, tf=r.packed, counters=r.counters, error=r.error,
-                px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep)
+                px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep, flags=tflags)
 
     for _ in range(args.warmup):
         step()
@@ -278,7 +282,7 @@ def run_ours(args):
             image.zero_()
             e0.record(stream)
             vrender(r.bricks, view, order, _lib.VOLUME_RENDER, image, tf=r.packed, counters=r.counters,
-                    error=r.error, px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep)
+                    error=r.error, px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep, flags=tflags)
             e1.record(stream)
             launches += 1
             times.append((e0, e1))
@@ -336,13 +340,14 @@ def run_ours(args):
         d2h = s.last_d2h_bytes
         e2e_v = samples_step / float(np.median(ets)) / 1e9
         e2e = {"value": e2e_v, "unit": "Gsamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": 1e3 * float(np.median(ets)), "path": "VolumeRenderSampler(...)(pg) per brick, aimage"}
+               "ms_per_step": 1e3 * float(np.median(ets)), "path": "VolumeRenderSampler(...)(pg) per brick, aimage",
+               "breakdown_ms": {k: round(v, 3) for k, v in s.last_timings.items()}}
         del out
 
     line = {"metric": "Gsamples/s", "value": value, "unit": "Gsamples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(ms.mean()), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 sampling / f64 traversal", "data": "synthetic",
-            "config": config_dict(w, args),
+            "config": {**config_dict(w, args), "tile_shape": tile_shape},
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
             "samples_per_step": samples_step, "rays_per_step": rays, "brick_walks_per_step": walks_step,
             "out_of_brick_cells_per_step": guarded_step,
@@ -398,6 +403,7 @@ def run_multiview(args):
 
     from yt_gb300 import _lib, workloads
     from yt_gb300.amr_kdtree import AMRKDTree
+    from yt_gb300.autotune import tile_shape_for
     from yt_gb300.batch import Batch, Job
     from yt_gb300.render import Renderer
 
@@ -408,7 +414,7 @@ def run_multiview(args):
     r_vr = Renderer(w.bricks, w.tf, device=dev, kdtree=w.kdtree)
     r_pj = Renderer(lin.bricks(), None, device=dev, kdtree=lin)
     t_build = time.time() - t0
-    ts = args.tile_shape if args.tile_shape >= 0 else 0
+    ts = args.tile_shape if args.tile_shape >= 0 else None
     jobs = [Job(r_vr if v.kind == _lib.VOLUME_RENDER else r_pj, v.camera, v.kind) for v in w.views]
     stream = torch.cuda.current_stream(dev)
     # plain: one launch per view, inputs resident (orders and rects prepared)
@@ -421,15 +427,17 @@ def run_multiview(args):
         order = rr.order(j.camera)
         rects = rr.bricks.rects(view, order)
         img = torch.zeros((*j.camera.resolution, 4), dtype=torch.float64, device=dev)
-        prepared.append((rr, view, order, rects, img, j.kind))
+        ctf = bool(j.kind == _lib.VOLUME_RENDER and rr.packed.header.ctf_fast)
+        vts = ts if ts is not None else tile_shape_for(j.kind, ctf, view.lens)
+        prepared.append((rr, view, order, rects, img, j.kind, vts))
     keep = []
 
     def plain():
-        for rr, view, order, rects, img, kind in prepared:
+        for rr, view, order, rects, img, kind, vts in prepared:
             img.zero_()
             vrender(rr.bricks, view, order, kind, img, tf=rr.packed if kind == _lib.VOLUME_RENDER else None,
                     counters=rr.counters, error=rr.error, stream=stream, rects=rects, keep=keep,
-                    flags=ts << _lib.FLAG_TILE_SHIFT)
+                    flags=vts << _lib.FLAG_TILE_SHIFT)
 
     b = Batch(jobs, device=dev, tile_shape=ts)
     graph = b.capture()
@@ -464,7 +472,8 @@ def run_multiview(args):
                       "p50_ms": float(np.percentile(ms_plain, 50)), "p99_ms": float(np.percentile(ms_plain, 99)),
                       "launches": len(jobs)},
             "batched": {"p50_ms": float(np.percentile(ms_batch, 50)), "p99_ms": float(np.percentile(ms_batch, 99)),
-                        "launches_per_graph": len(b.groups), "work_items": b.total_tiles, "tile_shape": ts},
+                        "launches_per_graph": len(b.groups), "work_items": b.total_tiles,
+                        "tile_shape": b.tile_shape},
             "samples_per_step": samples_batch, "samples_match": samples_batch == samples_plain,
             "roofline": {"bound": "hbm", "achieved": alg / (ms_batch.mean() / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
                          "frac": alg / (ms_batch.mean() / 1e3) / 1e9 / hbm},

@@ -240,6 +240,10 @@ int ytgb_pack_masks(const uint8_t *const *src, const int64_t *count, const int64
  * (an all-zero image needs no upload; an all-ones zbuffer equals none). */
 int ytgb_host_is_uniform(const double *x, int64_t n, double value, int32_t n_threads, int32_t *result);
 
+/* memcpy on up to n_threads host threads (<= 0: all cores): moves a
+ * rendered image from a pinned staging buffer into the caller's array. */
+int ytgb_host_copy(void *dst, const void *src, int64_t bytes, int32_t n_threads);
+
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
  * amr_kdtools.Node.add_grids / insert_grids / split_grids /

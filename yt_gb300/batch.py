@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .autotune import tile_shape_for
 from .render import Renderer
 
 
@@ -48,8 +49,18 @@ class _Group:
 
 
 class Batch:
-    def __init__(self, jobs, device="cuda", tile_shape=0, blocks=0):
+    def __init__(self, jobs, device="cuda", tile_shape=None, blocks=0):
+        """``tile_shape`` None: the tuned shape (``yt_gb300/tuning.json``) of
+        the class most of the jobs belong to."""
         self.device = torch.device(device)
+        if tile_shape is None:
+            votes = {}
+            for j in jobs:
+                tf = j.renderer.packed if j.kind == _lib.VOLUME_RENDER else None
+                lens = _lib.LENS_PLANE_PARALLEL if j.camera.lens_type == "plane-parallel" else _lib.LENS_PERSPECTIVE
+                ts = tile_shape_for(j.kind, bool(tf is not None and tf.header.ctf_fast), lens)
+                votes[ts] = votes.get(ts, 0) + 1
+            tile_shape = max(votes, key=votes.get) if votes else 0
         self.tile_shape = int(tile_shape)
         self.blocks = int(blocks)
         self.jobs = list(jobs)

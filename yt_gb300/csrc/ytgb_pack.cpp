@@ -149,3 +149,16 @@ extern "C" int ytgb_host_is_uniform(const double *x, int64_t n, double value, in
     for (int v : same) *result &= v;
     return YTGB_OK;
 }
+
+extern "C" int ytgb_host_copy(void *dst, const void *src, int64_t bytes, int32_t n_threads) {
+    if (bytes < 0 || (bytes > 0 && (!dst || !src))) {
+        ytgb_set_error("ytgb_host_copy: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    unsigned char *d = static_cast<unsigned char *>(dst);
+    const unsigned char *s = static_cast<const unsigned char *>(src);
+    parallel_ranges(bytes, thread_count(n_threads, bytes * 2), [&](int64_t lo, int64_t hi) {
+        if (hi > lo) std::memcpy(d + lo, s + lo, (size_t)(hi - lo));
+    });
+    return YTGB_OK;
+}

@@ -131,15 +131,29 @@ YTGB_HD float scaled_to_float(unsigned long long F, int k) {
     return ffrom(((uint32_t)(e + 127) << 23) | (uint32_t)(sig & 0x7fffffull));
 }
 
+// F * 2^k as float for F < 2^54: one rounding of F to float (the hardware
+// integer conversion, round to nearest even), then an exact scaling by a
+// power of two while the result stays in float's normal range; otherwise
+// the bit-level rounding above.  Both give the float nearest to F * 2^k.
+YTGB_HD float scaled_to_float_fast(unsigned long long F, int k) {
+    if (k < -126 || k > 127 - 54) return scaled_to_float(F, k);
+#ifdef __CUDA_ARCH__
+    const float f = __ull2float_rn(F);
+#else
+    const float f = (float)F;
+#endif
+    return fmul(f, ffrom((uint32_t)(k + 127) << 23));
+}
+
 // x - y as float for x >= y >= 0 given as float64 bit patterns: exact
 // integer difference when the exponents are equal or adjacent, else float64.
 YTGB_HD float diff_to_float_ordered(long long xb, long long yb) {
     const int ex = (int)(xb >> 52), ey = (int)(yb >> 52);
-    if (ey > 0 && ex == ey) return scaled_to_float((unsigned long long)(xb - yb), ex - 1075);
+    if (ey > 0 && ex == ey) return scaled_to_float_fast((unsigned long long)(xb - yb), ex - 1075);
     if (ey > 0 && ex == ey + 1) {
         const unsigned long long mx = (unsigned long long)((xb & MANT52) | (1LL << 52));
         const unsigned long long my = (unsigned long long)((yb & MANT52) | (1LL << 52));
-        return scaled_to_float(2 * mx - my, ey - 1075);
+        return scaled_to_float_fast(2 * mx - my, ey - 1075);
     }
     return (float)dsub(dfrom(xb), dfrom(yb));
 }
@@ -157,11 +171,11 @@ YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
     const unsigned long long m = (unsigned long long)((tb & MANT52) | (1LL << 52));
     if (e < 0) {
         fl = 0;
-        frac = scaled_to_float(m, e - 52);
+        frac = scaled_to_float_fast(m, e - 52);
     } else {
         const int sh = 52 - e;
         fl = (int)(m >> sh);
-        frac = scaled_to_float(m & ((1ull << sh) - 1), -sh);
+        frac = scaled_to_float_fast(m & ((1ull << sh) - 1), -sh);
     }
 }
 

@@ -19,6 +19,9 @@ explicitly.
 """
 from __future__ import annotations
 
+import ctypes as C
+import time
+
 import numpy as np
 import torch
 
@@ -86,10 +89,10 @@ def brick_tuple(pg):
     """(data, mask, left_edge, right_edge, dims) of a PartitionedGrid -- yt's
     own Cython object or :class:`yt_gb300.partitioned_grid.PartitionedGrid`.
     dims come from the mask, which has one entry per cell."""
-    data = list(pg.my_data)
-    mask = np.asarray(pg.source_mask)
-    dims = np.array(mask.shape, dtype=np.int64)
-    return data, mask, np.asarray(pg.LeftEdge, dtype=np.float64), np.asarray(pg.RightEdge, dtype=np.float64), dims
+    mask = pg.source_mask
+    if not isinstance(mask, np.ndarray):
+        mask = np.asarray(mask)
+    return list(pg.my_data), mask, pg.LeftEdge, pg.RightEdge, mask.shape
 
 
 class ImageSampler:
@@ -124,6 +127,7 @@ class ImageSampler:
         self.last_counters = None
         self.last_h2d_bytes = 0
         self.last_d2h_bytes = 0
+        self.last_timings = {}
 
     # ---- the call surface ---------------------------------------------------
     def __call__(self, pg, **kwa):
@@ -167,32 +171,64 @@ class ImageSampler:
             return
         pending, self._pending = self._pending, []
         dev = _device()
+        L = _lib.lib()
+        t0 = time.perf_counter()
         bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev)
         order = np.arange(len(pending), dtype=np.int32)
-        img = np.ascontiguousarray(self._image, dtype=np.float64)
-        image_d = torch.from_numpy(img).to(dev)
-        zb = torch.from_numpy(np.ascontiguousarray(self.azbuffer, dtype=np.float64)).to(dev)
+        nx, ny = self.nv
+        t1 = time.perf_counter()
+        # The caller's image, updated in place.  An image of zero bits (a new
+        # image) is cleared on the device instead of copied; a zbuffer of
+        # ones clips nothing (image_samplers.pyx:185, max_t = 1) and is left
+        # out.  Both checks read the host arrays once on all cores.
+        img = self._image
+        if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
+            img = np.ascontiguousarray(img, dtype=np.float64)
+        flag = C.c_int32()
+        _lib.check(L.ytgb_host_is_uniform(img.ctypes.data, img.size, 0.0, 0, C.byref(flag)), "image check")
+        h2d = 0
+        if flag.value:
+            image_d = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev)
+        else:
+            image_d = torch.from_numpy(img).to(dev)
+            h2d += img.nbytes
+        zb = np.ascontiguousarray(self.azbuffer, dtype=np.float64)
+        _lib.check(L.ytgb_host_is_uniform(zb.ctypes.data, zb.size, 1.0, 0, C.byref(flag)), "zbuffer check")
+        zb_d = None
+        if not flag.value:
+            zb_d = torch.from_numpy(zb).to(dev)
+            h2d += zb.nbytes
         px_pos = px_dir = None
         if self._px_pos is not None:
             px_pos = torch.from_numpy(self._px_pos).to(dev)
             px_dir = torch.from_numpy(self._px_dir).to(dev)
-        h2d = bricks.upload_bytes + img.nbytes + self.azbuffer.size * 8
-        if px_pos is not None:
-            h2d += 2 * self._px_pos.nbytes
+            h2d += self._px_pos.nbytes + self._px_dir.nbytes
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)
-        _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb,
+        torch.cuda.synchronize(dev)
+        t2 = time.perf_counter()
+        _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb_d,
                 n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
                 px_pos=px_pos, px_dir=px_dir)
         stream = torch.cuda.current_stream(dev)
-        _lib.check(_lib.lib().ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
-        out = image_d.cpu().numpy()
-        self._image[...] = out
+        _lib.check(L.ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
+        t3 = time.perf_counter()
+        # device -> pinned staging (full link speed), then into the caller's
+        # array on all host cores
+        stage = torch.empty(image_d.shape, dtype=torch.float64, pin_memory=True)
+        stage.copy_(image_d)
+        _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
+        if img is not self._image:
+            self._image[...] = img
         self.last_counters = counters.cpu().numpy()
+        t4 = time.perf_counter()
         # bytes copied host -> device (bricks, boundary tables, descriptors,
-        # image, zbuffer, per-pixel rays, order and rectangles) and back
-        self.last_h2d_bytes = int(h2d + 20 * len(pending))
-        self.last_d2h_bytes = int(out.nbytes + 4 * 8)
+        # masks, order and rectangles, and whichever of image, zbuffer and
+        # per-pixel rays were needed) and device -> host (image, counters)
+        self.last_h2d_bytes = int(bricks.upload_bytes + h2d + 20 * len(pending))
+        self.last_d2h_bytes = int(img.nbytes + 4 * 8)
+        self.last_timings = {"pack_ms": 1e3 * (t1 - t0), "upload_ms": 1e3 * (t2 - t1), "render_ms": 1e3 * (t3 - t2),
+                             "download_ms": 1e3 * (t4 - t3)}
 
     def ensure_code_unit_params(self, params):
         for name in ["center", "vp_pos", "vp_dir", "width"]:

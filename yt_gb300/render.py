@@ -12,6 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .autotune import tile_shape_for
 from .image_samplers import make_view
 from .transfer_functions import pack
 from .volume import BrickSet, render as _render, trace as _trace
@@ -45,8 +46,16 @@ class Renderer:
         return self.kdtree.viewpoint_order(camera.viewpoint)
 
     def render(self, camera, kind=_lib.VOLUME_RENDER, n_samples=1, order=None, image=None, zbuffer=None,
-               flags=0, stream=None, keep=None, device_rays=True):
+               flags=0, stream=None, keep=None, device_rays=True, tile_shape=None):
+        """Render one view.  ``tile_shape`` None takes the tuned shape of the
+        view's workload class (``yt_gb300/tuning.json``) unless ``flags``
+        already carries one."""
         view, ppos, pdir = self.view_args(camera, device_rays)
+        if tile_shape is None and not (flags >> _lib.FLAG_TILE_SHIFT) & 0xF:
+            ctf = bool(kind == _lib.VOLUME_RENDER and self.packed is not None and self.packed.header.ctf_fast)
+            tile_shape = tile_shape_for(kind, ctf, view.lens)
+        if tile_shape is not None:
+            flags = (flags & ~(0xF << _lib.FLAG_TILE_SHIFT)) | (int(tile_shape) << _lib.FLAG_TILE_SHIFT)
         nx, ny = camera.resolution
         if order is None:
             order = self.order(camera)

@@ -69,7 +69,7 @@ class _InFlight:
 
 class RenderServer:
     def __init__(self, volumes: dict, tfs: dict, device="cuda", hbm_budget=8 << 30, slots=4, max_batch=64,
-                 tile_shape=0, keep_images=False):
+                 tile_shape=None, keep_images=False):
         """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name -> transfer function."""
         self.device = torch.device(device)
         self.renderers = {}
