@@ -244,6 +244,14 @@ int ytgb_host_is_uniform(const double *x, int64_t n, double value, int32_t n_thr
  * rendered image from a pinned staging buffer into the caller's array. */
 int ytgb_host_copy(void *dst, const void *src, int64_t bytes, int32_t n_threads);
 
+/* Prefault the whole pages of a host array for writing without changing
+ * its contents (madvise MADV_POPULATE_WRITE).  A freshly allocated zero
+ * image that is read before it is written (the zero check above, yt's own
+ * read-modify-write) otherwise maps the kernel's shared zero page first and
+ * pays a copy-on-write fault per page on the write: on the Grace host that
+ * made writing a 32 MiB image ~12 ms instead of ~0.7 ms. */
+int ytgb_host_prefault(void *p, int64_t bytes);
+
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
  * amr_kdtools.Node.add_grids / insert_grids / split_grids /

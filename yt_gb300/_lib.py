@@ -146,6 +146,7 @@ SIGNATURES = {
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                   C.POINTER(C.c_int32)]),
     "ytgb_host_copy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
+    "ytgb_host_prefault": (C.c_int, [C.c_void_p, C.c_int64]),
     "ytgb_host_is_uniform": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_int32, C.POINTER(C.c_int32)]),
     "ytgb_kdtree_build": (C.c_void_p, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_kdtree_destroy": (None, [C.c_void_p]),

@@ -7,6 +7,9 @@
 // gather is split over the host's cores.  The float64 -> float32 conversion
 // is the C++ cast (round to nearest even), the same rounding as numpy's
 // astype(float32).
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -19,8 +22,10 @@
 
 namespace {
 
+// Default: up to 8 threads.  These loops are memory-bound; on the 16-core
+// Grace host a 32 MiB copy ran in 0.46 ms on 4-8 threads and 0.85 ms on 16.
 int thread_count(int32_t requested, int64_t work_bytes) {
-    int t = requested > 0 ? requested : (int)std::thread::hardware_concurrency();
+    int t = requested > 0 ? requested : std::min(8, (int)std::thread::hardware_concurrency());
     if (t < 1) t = 1;
     if (t > 64) t = 64;
     // at least ~1 MiB per thread: below that, thread start-up dominates
@@ -160,5 +165,25 @@ extern "C" int ytgb_host_copy(void *dst, const void *src, int64_t bytes, int32_t
     parallel_ranges(bytes, thread_count(n_threads, bytes * 2), [&](int64_t lo, int64_t hi) {
         if (hi > lo) std::memcpy(d + lo, s + lo, (size_t)(hi - lo));
     });
+    return YTGB_OK;
+}
+
+// MADV_POPULATE_WRITE (Linux 5.14) where the C library headers predate it.
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
+
+extern "C" int ytgb_host_prefault(void *p, int64_t bytes) {
+    if (bytes < 0 || (bytes > 0 && !p)) {
+        ytgb_set_error("ytgb_host_prefault: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    const long page = sysconf(_SC_PAGESIZE);
+    if (page <= 0 || bytes == 0) return YTGB_OK;
+    const uintptr_t a = (uintptr_t)p, e = a + (uintptr_t)bytes;
+    const uintptr_t lo = (a + page - 1) / page * page, hi = e / page * page;
+    // whole pages inside [p, p + bytes) only; failure (older kernel, an
+    // unusual mapping) just leaves the pages to fault on first write
+    if (hi > lo) (void)madvise((void *)lo, hi - lo, MADV_POPULATE_WRITE);
     return YTGB_OK;
 }

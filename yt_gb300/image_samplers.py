@@ -20,6 +20,7 @@ explicitly.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import time
 
 import numpy as np
@@ -34,6 +35,20 @@ def _device():
     if not torch.cuda.is_available():
         raise _lib.YtgbError("yt_gb300 samplers need a CUDA device (there is no CPU fallback)")
     return torch.device("cuda", torch.cuda.current_device())
+
+
+_stage = {"buf": None, "lock": threading.Lock()}
+
+
+def _staging(nbytes: int) -> torch.Tensor:
+    """A page-locked float64 host buffer of at least ``nbytes``, kept for
+    reuse (grown as needed).  flush() holds ``_stage["lock"]`` while it uses
+    it."""
+    b = _stage["buf"]
+    if b is None or b.numel() * 8 < nbytes:
+        b = torch.empty((nbytes + 7) // 8, dtype=torch.float64, pin_memory=True)
+        _stage["buf"] = b
+    return b
 
 
 def make_view(vp_pos, vp_dir, center, bounds, nx, ny, x_vec, y_vec, width, lens_type, camera_data):
@@ -185,6 +200,10 @@ class ImageSampler:
         if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
             img = np.ascontiguousarray(img, dtype=np.float64)
         flag = C.c_int32()
+        # the result is written into img below: fault its pages in for
+        # writing first, so that reading it here does not map the shared
+        # zero page (and make every page a copy-on-write fault later)
+        _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
         _lib.check(L.ytgb_host_is_uniform(img.ctypes.data, img.size, 0.0, 0, C.byref(flag)), "image check")
         h2d = 0
         if flag.value:
@@ -215,9 +234,10 @@ class ImageSampler:
         t3 = time.perf_counter()
         # device -> pinned staging (full link speed), then into the caller's
         # array on all host cores
-        stage = torch.empty(image_d.shape, dtype=torch.float64, pin_memory=True)
-        stage.copy_(image_d)
-        _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
+        with _stage["lock"]:
+            stage = _staging(img.nbytes)[: img.size].view(image_d.shape)
+            stage.copy_(image_d)
+            _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
         if img is not self._image:
             self._image[...] = img
         self.last_counters = counters.cpu().numpy()

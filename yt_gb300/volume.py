@@ -21,10 +21,19 @@ from . import _lib
 
 
 def _pinned(shape, dtype, device) -> torch.Tensor:
-    t = torch.empty(shape, dtype=dtype)
-    if torch.device(device).type == "cuda":
-        t = t.pin_memory()
-    return t
+    # page-locked host memory from torch's caching host allocator (reused
+    # across calls) when the destination is a GPU
+    return torch.empty(shape, dtype=dtype, pin_memory=torch.device(device).type == "cuda")
+
+
+def _address(a: np.ndarray) -> int:
+    """Data address of a C-contiguous array (through the buffer protocol,
+    which is cheaper than ``a.ctypes.data``; read-only arrays take the slow
+    path)."""
+    try:
+        return C.addressof(C.c_char.from_buffer(a))
+    except (TypeError, ValueError):
+        return a.ctypes.data
 
 
 # numpy view of ytgb_brick (include/ytgb.h), field for field
@@ -53,23 +62,32 @@ class BrickSet:
         m = max(n, 1)
         desc = np.zeros(m, dtype=BRICK_DTYPE)
         f64 = np.dtype(np.float64)
+        u8 = np.dtype(np.uint8)
         dims_l, le_l, re_l, nf_l = [], [], [], []
-        fields = []     # float64 C-contiguous arrays, all bricks' fields in order
-        masks = []      # (brick, uint8 C-contiguous mask)
+        keep = []                      # arrays whose addresses are taken
+        fptr, fsz = [], []             # every field of every brick, in order
+        mk_k, mptr, msz = [], [], []   # bricks with a mask
+        addr = _address
         for k, (data, mask, le_k, re_k, dims_k) in enumerate(bricks):
             dims_l.append(dims_k)
-            le_l.append(le_k[:3])
-            re_l.append(re_k[:3])
+            le_l.append(le_k)
+            re_l.append(re_k)
             nf_l.append(len(data))
             for d in data:
                 if not (type(d) is np.ndarray and d.dtype == f64 and d.flags.c_contiguous):
                     d = np.ascontiguousarray(d, dtype=np.float64)
-                fields.append(d)
+                keep.append(d)
+                fptr.append(addr(d))
+                fsz.append(d.size)
             if mask is not None:
-                mk = np.asarray(mask)
-                if mk.dtype == np.bool_:
-                    mk = mk.view(np.uint8)
-                masks.append((k, np.ascontiguousarray(mk, dtype=np.uint8)))
+                mk = mask
+                if not (type(mk) is np.ndarray and mk.dtype == u8 and mk.flags.c_contiguous):
+                    mk = np.asarray(mk)
+                    mk = np.ascontiguousarray(mk.view(np.uint8) if mk.dtype == np.bool_ else mk, dtype=np.uint8)
+                keep.append(mk)
+                mk_k.append(k)
+                mptr.append(addr(mk))
+                msz.append(mk.size)
         dims = np.ones((m, 3), dtype=np.int64)
         le = np.zeros((m, 3))
         re = np.ones((m, 3))
@@ -79,21 +97,21 @@ class BrickSet:
                 dims[:n] = np.array(dims_l, dtype=np.int64).reshape(n, 3)
             except ValueError:
                 raise ValueError("brick dims must be 3 positive integers") from None
-            le[:n] = np.array(le_l, dtype=np.float64)
-            re[:n] = np.array(re_l, dtype=np.float64)
+            le[:n] = np.array(le_l, dtype=np.float64).reshape(n, -1)[:, :3]
+            re[:n] = np.array(re_l, dtype=np.float64).reshape(n, -1)[:, :3]
             nfields[:n] = nf_l
         bad = np.nonzero((dims[:n] <= 0).any(axis=1) | (nfields[:n] < 1) | (nfields[:n] > 6))[0]
         if bad.size:
             k = int(bad[0])
             raise ValueError(f"brick {k}: dims must be 3 positive integers and 1 to 6 fields are supported "
                              f"(dims {dims[k].tolist()}, {int(nfields[k])} fields)")
-        if masks:
-            mk_brick = np.array([k for k, _ in masks], dtype=np.int64)
-            mk_size = np.array([mk.size for _, mk in masks], dtype=np.int64)
+        if mk_k:
+            mk_brick = np.array(mk_k, dtype=np.int64)
+            mk_size = np.array(msz, dtype=np.int64)
             wrong = np.nonzero(mk_size != dims[mk_brick].prod(axis=1))[0]
             if wrong.size:
                 raise ValueError(f"brick {int(mk_brick[wrong[0]])}: mask must have prod(dims) entries")
-        fsize = np.array([a.size for a in fields], dtype=np.int64)
+        fsize = np.array(fsz, dtype=np.int64)
         fstart = np.concatenate([[0], np.cumsum(nfields[:n])]).astype(np.int64)
         sizes_min = np.minimum.reduceat(fsize, fstart[:-1]) if n else fsize
         sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
@@ -135,25 +153,25 @@ class BrickSet:
         buf = _pinned((max(total, 4),), torch.float32, self.device)
         L = _lib.lib()
         # float64 -> float32 gather into the pinned arena, on all host cores
-        src = np.array([a.ctypes.data for a in fields], dtype=np.uintp)
+        src = np.array(fptr, dtype=np.uintp)
         fbrick = np.repeat(np.arange(n), nfields[:n])
-        dst_f = (data_off[fbrick] + (np.arange(len(fields)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
-        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fields),
+        dst_f = (data_off[fbrick] + (np.arange(len(fptr)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
+        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
                                       buf.data_ptr(), 0), "ytgb_pack_fields")
         # masks: kept only when some cell is masked out
         mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
         desc["mask_offset"][:] = -1
         mbuf = None
-        if masks:
-            msrc = np.array([mk.ctypes.data for _, mk in masks], dtype=np.uintp)
+        if mk_k:
+            msrc = np.array(mptr, dtype=np.uintp)
             mcnt = mk_size
             mdst = mstart[mk_brick]
             ones = C.c_int32()
-            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(masks), None, 0,
+            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k), None, 0,
                                          C.byref(ones)), "ytgb_pack_masks")
             if not ones.value:
                 mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
-                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(masks),
+                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k),
                                              mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
                 desc["mask_offset"][mk_brick] = mdst
         self.desc_host = desc
