@@ -48,11 +48,11 @@ def parse():
     ap.add_argument("--cpu-res", type=int, default=0, help="resolution of the CPU-baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="amr_vr", choices=["amr_vr", "multiview", "projection", "serve"],
+    ap.add_argument("--workload", default="amr_vr", choices=["amr_vr", "multiview", "projection", "serve", "prep"],
                     help="amr_vr (default, the headline frame); the others print their own line")
     ap.add_argument("--tile-shape", type=int, default=-1, help="-1: from the autotuning table")
-    ap.add_argument("--n-requests", type=int, default=2000)
-    ap.add_argument("--rates", default="50,100,200,500,1000,2000")
+    ap.add_argument("--n-requests", type=int, default=400)
+    ap.add_argument("--rates", default="50,100,200,400")
     return ap.parse_args()
 
 
@@ -128,6 +128,9 @@ def build_workload(args):
     return w, time.time() - t
 
 
+_SAMPLE_COUNTS = {}
+
+
 def cpu_reference(w, res, threads):
     """Time yt's compiled sampler (or the C oracle) over the view at ``res``."""
     from yt_gb300.camera import Camera
@@ -159,13 +162,17 @@ def cpu_reference(w, res, threads):
         dt = time.perf_counter() - t0
         image = np.array(s.aimage)
         kind = "reference"
-        from oracle import cpu as ocpu  # noqa: PLC0415   the visit count comes from the oracle
+        key = (res, len(w.bricks))
+        samples = _SAMPLE_COUNTS.get(key)
+        if samples is None:
+            # the visit count comes from the oracle's trace (same walk), once per sample view
+            from oracle import cpu as ocpu  # noqa: PLC0415
 
-        so = ocpu.OracleSampler("volume_render", p["vp_pos"], p["vp_dir"], p["center"], p["bounds"],
-                                np.zeros_like(p["image"]), p["x_vec"], p["y_vec"], p["width"],
-                                lens_type=p["lens_type"], camera_data=p["camera_data"], tf=w.tf)
-        _, counts = so.trace(ocpu.OracleBricks(w.bricks), order, num_threads=threads)
-        samples = int(counts.sum())
+            so = ocpu.OracleSampler("volume_render", p["vp_pos"], p["vp_dir"], p["center"], p["bounds"],
+                                    np.zeros_like(p["image"]), p["x_vec"], p["y_vec"], p["width"],
+                                    lens_type=p["lens_type"], camera_data=p["camera_data"], tf=w.tf)
+            _, counts = so.trace(ocpu.OracleBricks(w.bricks), order, num_threads=threads)
+            samples = _SAMPLE_COUNTS[key] = int(counts.sum())
     except ImportError:
         from oracle import cpu as ocpu  # noqa: PLC0415
 
@@ -589,6 +596,9 @@ def run_serve(args):
         lo, hi = sorted(rng.uniform(-0.3, 1.6, 2))
         tfs[f"tf{k}"] = workloads.color_tf((lo - 0.2, hi + 0.2), int(rng.integers(3, 9)))
     srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=4, max_batch=64)
+    # the plain form: the same server one request per launch on one stream
+    plain_srv = RenderServer({}, {}, device=dev, hbm_budget=16 << 30, slots=1, max_batch=1)
+    plain_srv.volumes, plain_srv.tfs = srv.volumes, srv.tfs
     t_build = time.time() - t0
     sizes = (256, 512, 1024, 2048)
 
@@ -612,23 +622,36 @@ def run_serve(args):
 
     # warm-up: compile paths, stage tables
     srv.run(make(16, 1e6, 99), realtime=False)
+    plain_srv.run(make(4, 1e6, 98), realtime=False)
     results = []
     rates = [float(x) for x in args.rates.split(",")]
     total_samples = 0
     total_busy = 0.0
     audit = []
     for k, rate in enumerate(rates):
-        reqs = make(args.n_requests, rate, 1000 + k)
-        srv.samples = 0
+        row = {"rate_req_s": rate}
+        for label, server in (("served", srv), ("plain", plain_srv)):
+            reqs = make(args.n_requests, rate, 1000 + k)
+            server.samples = 0
+            t = time.perf_counter()
+            done = server.run(reqs, realtime=True)
+            wall = time.perf_counter() - t
+            row[label] = {**latency_summary(done), "Gsamples/s": server.samples / wall / 1e9, "wall_s": wall,
+                          "samples": server.samples}
+            if label == "served":
+                total_samples += server.samples
+                total_busy += wall
+                audit += [q for q in done if q.rid % 100 == 0]
+        results.append(row)
+    # closed loop (every request available at once): throughput bound of each form
+    closed = {}
+    for label, server in (("served", srv), ("plain", plain_srv)):
+        reqs = make(args.n_requests, 1e9, 77)
+        server.samples = 0
         t = time.perf_counter()
-        done = srv.run(reqs, realtime=True)
+        done = server.run(reqs, realtime=False)
         wall = time.perf_counter() - t
-        lat = latency_summary(done)
-        results.append({"rate_req_s": rate, **lat, "Gsamples/s": srv.samples / wall / 1e9,
-                        "wall_s": wall, "samples": srv.samples})
-        total_samples += srv.samples
-        total_busy += wall
-        audit += [q for q in done if q.rid % 100 == 0]
+        closed[label] = {**latency_summary(done), "Gsamples/s": server.samples / wall / 1e9, "wall_s": wall}
     # 1% audit against the float64 oracle (smallest images of the audit set)
     audit = sorted(audit, key=lambda q: np.prod(q.camera.resolution))[:8]
     errs = []
@@ -648,12 +671,69 @@ def run_serve(args):
         s.render(ocpu.OracleBricks(bricks), order, num_threads=os.cpu_count() or 1)
         errs.append(relative_error(img, p["image"], channels=(0, 1, 2) if q.kind == 0 else (0,))[0])
     line = {"metric": "Gsamples/s & p50/p99 latency", "workload": "serve",
-            "value": total_samples / total_busy / 1e9, "unit": "Gsamples/s", "n_gpus": 1,
-            "higher_is_better": True, "rates": results,
+            "value": closed["served"]["Gsamples/s"], "unit": "Gsamples/s", "n_gpus": 1,
+            "higher_is_better": True, "rates": results, "closed_loop": closed,
             "audit": {"n": len(errs), "max_rel_err": float(max(errs)) if errs else None},
             "config": {"volumes": {k: len(v[0]) for k, v in vols.items()}, "tfs": 16, "sizes": list(sizes),
-                       "requests_per_rate": args.n_requests, "slots": 4, "max_batch": 64},
+                       "requests_per_rate": args.n_requests, "slots": 4, "max_batch": 64,
+                       "plain": "same server, one request per launch, one stream"},
             "build_seconds": t_build}
+    print(json.dumps(line), flush=True)
+
+
+def run_prep(args):
+    """Time to first image's brick preparation for the AMR dataset: yt's
+    host path (numpy vertex centring, log10, per-leaf slicing, then packing
+    and upload) against the device path (cell data uploaded once, bricks
+    computed by ytgb_vertex_bricks), each from the grids to a resident
+    BrickSet; then one render from each, compared bit for bit."""
+    import torch
+
+    from yt_gb300 import testing, workloads
+    from yt_gb300.amr_kdtree import AMRKDTree
+    from yt_gb300.render import Renderer
+    from yt_gb300.volume import BrickSet
+
+    dev = torch.device("cuda", 0)
+    grids = testing.amr_blob_grids(root=args.root, levels=args.levels, patch=16, seed=0)
+    w = workloads.amr_vr(root=args.root, levels=args.levels, res=args.res)
+    out = {"host_ms": [], "device_ms": [], "kd_ms": []}
+    bs_h = bs_d = kd = None
+    for i in range(args.warmup + max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kd = AMRKDTree(grids, log_field=True)
+        t1 = time.perf_counter()
+        bs_h = BrickSet(kd.bricks(), device=dev)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        kd2 = AMRKDTree(grids, log_field=True)
+        t3 = time.perf_counter()
+        bs_d = kd2.device_brickset(dev)
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        if i >= args.warmup:
+            out["kd_ms"].append(1e3 * (t1 - t0))
+            out["host_ms"].append(1e3 * (t2 - t1))
+            out["device_ms"].append(1e3 * (t4 - t3))
+    def valid(bs):
+        arena = bs.data.cpu().numpy()
+        off = bs.desc_host["data_offset"][: bs.n]
+        return np.concatenate([arena[o: o + v] for o, v in zip(off, bs.verts[: bs.n])]).view(np.int32)
+
+    vh, vd = valid(bs_h), valid(bs_d)
+    same_data = bool(np.array_equal(vh, vd))
+    n_diff = int((vh != vd).sum())
+    cam = w.views[0].camera
+    a = Renderer(bs_h, w.tf, device=dev, kdtree=kd).render(cam)
+    b = Renderer(bs_d, w.tf, device=dev, kdtree=kd).render(cam)
+    line = {"metric": "brick preparation ms", "workload": "prep", "value": float(np.median(out["device_ms"])),
+            "unit": "ms", "higher_is_better": False, "host_ms": float(np.median(out["host_ms"])),
+            "kd_build_ms": float(np.median(out["kd_ms"])), "bricks": bs_d.n, "grids": len(grids),
+            "arena_identical": same_data, "arena_values_differing": n_diff, "arena_values": int(vh.size),
+            "image_identical": bool(torch.equal(a.view(torch.int64), b.view(torch.int64))),
+            "device_upload_bytes": getattr(kd2, "device_upload_bytes", None),
+            "config": {"workload": f"{args.root}^3 root + {args.levels} levels, 16^3 patches, log10 field"}}
     print(json.dumps(line), flush=True)
 
 
@@ -667,5 +747,7 @@ if __name__ == "__main__":
         run_projection(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "prep":
+        run_prep(a)
     else:
         run_ours(a)

@@ -222,6 +222,23 @@ int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int3
                               int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t blocks,
                               void *stream);
 
+/* ---- device: brick preparation ------------------------------------------ */
+/* Replaces the per-leaf host work of AMRKDTree.get_brick_data
+ * (amr_kdtree.py:325-374): vertex centring of the leaf's grid
+ * (ghost_zone_interpolate without ghost zones, interpolators.pyx:177-226,
+ * grid_patch.py:270-296), log10 with values <= 0 -> NaN when log_field, and
+ * the slice [li:ri+1], written as float32 into field `field` of each brick's
+ * arena slot.  All arrays are device arrays: d_cells holds every grid's
+ * float64 cell data (C order) at d_grid_offset[g] with dims d_grid_dims[3g..];
+ * brick b takes grid d_brick_grid[b] from vertex d_brick_lo[3b..] with the
+ * dims and arena slot of d_bricks[b].  Every index is checked on the device;
+ * a brick that does not fit is skipped and YTGB_DEVERR_BAD_BRICK is written
+ * to *d_error (read it with ytgb_check_error). */
+int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const int64_t *d_grid_offset,
+                       const int32_t *d_grid_dims, int32_t n_grids, const int32_t *d_brick_grid,
+                       const int32_t *d_brick_lo, const ytgb_brick *d_bricks, int32_t n_bricks, int32_t field,
+                       int32_t log_field, float *d_arena, int64_t arena_len, int32_t *d_error, void *stream);
+
 /* ---- host: brick marshalling -------------------------------------------- */
 /* No reference counterpart: yt's sampler reads each PartitionedGrid's
  * float64 arrays in place (image_samplers.pyx:146-197, partitioned_grid.pyx:

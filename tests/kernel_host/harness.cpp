@@ -8,6 +8,7 @@
 #include <vector>
 #include "ytgb.h"
 #include "ytgb_ray.cuh"
+#include "ytgb_vertex.cuh"
 using namespace ytgb;
 
 template <int MODE, int CTF>
@@ -129,4 +130,13 @@ extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
         }
     }
     return bad;
+}
+
+// Every vertex of a C-order cell block, as the device brick preparation
+// computes it (ytgb_vertex.cuh).
+extern "C" void emu_vertex(const double *cells, int n0, int n1, int n2, double *out) {
+    long long t = 0;
+    for (int i = 0; i <= n0; i++)
+        for (int j = 0; j <= n1; j++)
+            for (int k = 0; k <= n2; k++) out[t++] = ytgb::vertex_value(cells, n0, n1, n2, i, j, k);
 }

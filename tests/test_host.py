@@ -249,3 +249,18 @@ def test_batch_tables_are_aligned_for_every_view():
     for g in b.groups:
         for k in range(g.n):
             assert g.entries[k].args.rects % 16 == 0
+
+
+def test_leaf_slices_match_brick():
+    from yt_gb300.amr_kdtree import AMRKDTree
+
+    kd = AMRKDTree(testing.amr_blob_grids(root=32, levels=2, patch=8, seed=3), log_field=True)
+    lg, li, dims = kd.leaf_slices()
+    for k in range(0, kd.num_bricks, 7):
+        data, mask, le, re, d = kd.brick(k)
+        g = kd.grids[lg[k]]
+        assert g.id == kd.leaf_grid[k]
+        assert np.array_equal(d, dims[k])
+        v = kd._vertex(g)
+        s = v[li[k][0]: li[k][0] + d[0] + 1, li[k][1]: li[k][1] + d[1] + 1, li[k][2]: li[k][2] + d[2] + 1]
+        assert np.array_equal(s, data[0], equal_nan=True)

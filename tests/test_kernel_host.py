@@ -35,7 +35,8 @@ TOL = 1e-5
 def emu():
     src = HERE / "harness.cpp"
     out = HERE / "_build" / "libytgb_host_walk.so"
-    deps = [src, ROOT / "yt_gb300" / "csrc" / "ytgb_ray.cuh", ROOT / "include" / "ytgb.h",
+    deps = [src, ROOT / "yt_gb300" / "csrc" / "ytgb_ray.cuh", ROOT / "yt_gb300" / "csrc" / "ytgb_vertex.cuh",
+            ROOT / "include" / "ytgb.h",
             ROOT / "yt_gb300" / "csrc" / "ytgb_internal.h"]
     if not out.exists() or out.stat().st_mtime < max(d.stat().st_mtime for d in deps):
         out.parent.mkdir(exist_ok=True)
@@ -250,3 +251,20 @@ def test_integer_conversions_match(emu):
     emu.emu_check_convert.restype = C.c_longlong
     emu.emu_check_convert.argtypes = [C.c_longlong, C.c_ulonglong]
     assert emu.emu_check_convert(1_000_000, 2) == 0
+
+
+def test_device_vertex_centring_matches_host(emu):
+    """The device brick preparation's vertex value (ytgb_vertex.cuh) equals
+    vertex_centred (itself pinned to the reference's ghost_zone_interpolate)
+    bit for bit, on grids from 2 cells per axis up, with negative, zero and
+    non-finite cells."""
+    emu.emu_vertex.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(4)
+    for shape in [(2, 2, 2), (2, 3, 5), (7, 4, 9), (16, 16, 16), (33, 9, 17)]:
+        cells = rng.lognormal(0.0, 2.0, shape) * rng.choice([-1.0, 1.0], shape)
+        cells.flat[rng.integers(0, cells.size, 3)] = [0.0, np.inf, np.nan]
+        cells = np.ascontiguousarray(cells)
+        out = np.empty(tuple(n + 1 for n in shape))
+        emu.emu_vertex(cells.ctypes.data, *shape, out.ctypes.data)
+        want = vertex_centred(cells)
+        assert np.array_equal(out.view(np.int64), want.view(np.int64)), shape

@@ -142,6 +142,9 @@ SIGNATURES = {
                                     C.c_void_p, C.c_int32, C.c_void_p]),
     "ytgb_batch_render_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                             C.c_int32, C.c_int32, C.c_void_p]),
+    "ytgb_vertex_bricks": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                     C.c_int64, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                   C.POINTER(C.c_int32)]),

@@ -133,6 +133,62 @@ class AMRKDTree:
             self._bricks = [self.brick(k) for k in range(self.num_bricks)]
         return self._bricks
 
+    def leaf_slices(self):
+        """(grid index, li, dims) of every leaf: the slice get_brick_data
+        takes from its grid (amr_kdtree.py:329-335)."""
+        gidx = {g.id: i for i, g in enumerate(self.grids)}
+        lg = np.array([gidx[int(i)] for i in self.leaf_grid], dtype=np.int32)
+        dds = np.array([np.asarray(g.dds, dtype=np.float64) for g in self.grids]).reshape(-1, 3)[lg]
+        gle = self._gles[lg]
+        li = np.rint((self.leaf_le - gle) / dds).astype("int32")
+        ri = np.rint((self.leaf_re - gle) / dds).astype("int32")
+        return lg, li, (ri - li).astype(np.int64)
+
+    def device_brickset(self, device="cuda", stream=None):
+        """The bricks as a :class:`~yt_gb300.volume.BrickSet` prepared on the
+        device: the grids' cell data is uploaded once and every leaf's
+        vertex-centred (and log10'd) slice is computed there
+        (``ytgb_vertex_bricks``) instead of on the host (:meth:`brick`).
+        The vertex values are bit-identical to the host path's; with
+        ``log_field`` the device log10 may differ from numpy's in the last
+        float64 bit, which reaches the float32 brick value only when it sits
+        on a float32 rounding boundary."""
+        import torch
+
+        from .volume import BrickSet, _pinned
+
+        dev = torch.device(device)
+        lg, li, dims = self.leaf_slices()
+        gshape = np.array([np.shape(g.data) for g in self.grids], dtype=np.int64).reshape(-1, 3)
+        if (gshape < 2).any():
+            raise ValueError("device brick preparation needs grids of at least 2 cells per axis")
+        if (li < 0).any() or (li + dims > gshape[lg]).any():
+            raise ValueError("a kd leaf does not lie inside its grid")
+        bs = BrickSet.on_device(dims, self.leaf_le, self.leaf_re, dev)
+        gsize = gshape.prod(axis=1)
+        goff = np.concatenate([[0], np.cumsum(gsize)]).astype(np.int64)
+        host = _pinned((max(int(goff[-1]), 1),), torch.float64, dev)
+        hnp = host.numpy()
+        for k, g in enumerate(self.grids):
+            hnp[goff[k]: goff[k + 1]] = np.asarray(g.data, dtype=np.float64).ravel()
+        s = stream or torch.cuda.current_stream(dev)
+        with torch.cuda.stream(s):
+            cells = host.to(dev, non_blocking=True)
+            meta_i64 = torch.from_numpy(goff[:-1].copy()).to(dev, non_blocking=False)
+            meta_i32 = torch.from_numpy(np.concatenate([gshape.ravel(), lg, li.ravel()]).astype(np.int32)).to(dev)
+        error = torch.zeros(1, dtype=torch.int32, device=dev)
+        ng, nb = len(self.grids), int(lg.size)
+        base = meta_i32.data_ptr()
+        L = _lib.lib()
+        _lib.check(L.ytgb_vertex_bricks(cells.data_ptr(), int(goff[-1]), meta_i64.data_ptr(), base, ng,
+                                        base + 4 * 3 * ng, base + 4 * (3 * ng + nb), bs.desc.data_ptr(), nb, 0,
+                                        int(bool(self.log_field)), bs.data.data_ptr(), bs.data.numel(),
+                                        error.data_ptr(), C.c_void_p(s.cuda_stream)), "ytgb_vertex_bricks")
+        _lib.check(L.ytgb_check_error(error.data_ptr(), s.cuda_stream), "ytgb_vertex_bricks")
+        self.device_upload_bytes = int(cells.numel() * 8 + meta_i64.numel() * 8 + meta_i32.numel() * 4 +
+                                       bs.upload_bytes)
+        return bs
+
     def traverse(self, viewpoint=None):
         """PartitionedGrid bricks in kd order (AMRKDTree.traverse, :248-250)."""
         order = range(self.num_bricks) if viewpoint is None else self.viewpoint_order(viewpoint)

@@ -1,0 +1,95 @@
+// ytgb_prep.cu -- device brick preparation (vertex centring, log10, slicing).
+//
+// Replaces the host loop of yt's AMRKDTree.get_brick_data
+// (amr_kdtree.py:325-374) over every kd leaf: one block per brick computes
+// the brick's (dims+1)^3 vertex values from its grid's cell data
+// (ytgb_vertex.cuh), applies log10 where requested and writes them as
+// float32 into the brick's slot of the arena.  Every index the kernel forms
+// is checked against the sizes it is given; a brick that does not fit its
+// grid or the arena is skipped and reported through the error word.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "ytgb.h"
+#include "ytgb_internal.h"
+#include "ytgb_vertex.cuh"
+
+namespace {
+
+using namespace ytgb;
+
+constexpr int PREP_BLOCK = 256;
+
+__global__ void __launch_bounds__(PREP_BLOCK)
+vertex_bricks_kernel(const double *cells, int64_t n_cells, const int64_t *grid_offset, const int32_t *grid_dims,
+                     int32_t n_grids, const int32_t *brick_grid, const int32_t *brick_lo, const ytgb_brick *bricks,
+                     int32_t field, int32_t log_field, float *arena, int64_t arena_len, int32_t *error) {
+    const int b = blockIdx.x;
+    const int g = brick_grid[b];
+    if (g < 0 || g >= n_grids) {
+        if (threadIdx.x == 0) set_error(error, YTGB_DEVERR_BAD_BRICK);
+        return;
+    }
+    const int n0 = grid_dims[3 * g], n1 = grid_dims[3 * g + 1], n2 = grid_dims[3 * g + 2];
+    const int l0 = brick_lo[3 * b], l1 = brick_lo[3 * b + 1], l2 = brick_lo[3 * b + 2];
+    const ytgb_brick &bk = bricks[b];
+    const int d0 = bk.dims[0], d1 = bk.dims[1], d2 = bk.dims[2];
+    const long long go = grid_offset[g];
+    const long long nv = (long long)(d0 + 1) * (d1 + 1) * (d2 + 1);
+    const long long out0 = bk.data_offset + (long long)field * bk.field_stride;
+    // the leaf's vertices [l, l + d] must be vertices of the grid [0, n], the
+    // grid's cells must lie in the cell array, and the slot in the arena
+    const bool ok = n0 >= 2 && n1 >= 2 && n2 >= 2 && d0 > 0 && d1 > 0 && d2 > 0 && l0 >= 0 && l1 >= 0 &&
+                    l2 >= 0 && l0 + d0 <= n0 && l1 + d1 <= n1 && l2 + d2 <= n2 && go >= 0 &&
+                    go + (long long)n0 * n1 * n2 <= n_cells && field >= 0 && field < bk.n_fields && out0 >= 0 &&
+                    out0 + nv <= arena_len && nv <= bk.field_stride;
+    if (!ok) {
+        if (threadIdx.x == 0) set_error(error, YTGB_DEVERR_BAD_BRICK);
+        return;
+    }
+    const double *c = cells + go;
+    float *out = arena + out0;
+    const int e1 = d1 + 1, e2 = d2 + 1;
+    for (long long t = threadIdx.x; t < nv; t += PREP_BLOCK) {
+        const int k = (int)(t % e2);
+        const long long r = t / e2;
+        const int j = (int)(r % e1);
+        const int i = (int)(r / e1);
+        double v = vertex_value(c, n0, n1, n2, l0 + i, l1 + j, l2 + k);
+        if (log_field) v = v <= 0.0 ? nan("") : log10(v);
+        out[t] = (float)v;
+    }
+}
+
+}  // namespace
+
+extern "C" int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const int64_t *d_grid_offset,
+                                  const int32_t *d_grid_dims, int32_t n_grids, const int32_t *d_brick_grid,
+                                  const int32_t *d_brick_lo, const ytgb_brick *d_bricks, int32_t n_bricks,
+                                  int32_t field, int32_t log_field, float *d_arena, int64_t arena_len,
+                                  int32_t *d_error, void *stream) {
+    if (n_bricks < 0 || n_grids < 0 || n_cells < 0 || arena_len < 0 || field < 0 || field > 5) {
+        ytgb_set_error("ytgb_vertex_bricks: bad sizes");
+        return YTGB_ERR_INVALID;
+    }
+    if (n_bricks == 0) return YTGB_OK;
+    if (!d_cells || !d_grid_offset || !d_grid_dims || !d_brick_grid || !d_brick_lo || !d_bricks || !d_arena ||
+        ((uintptr_t)d_cells & 7) || ((uintptr_t)d_grid_offset & 7) || ((uintptr_t)d_grid_dims & 3) ||
+        ((uintptr_t)d_brick_grid & 3) || ((uintptr_t)d_brick_lo & 3) || ((uintptr_t)d_bricks & 7) ||
+        ((uintptr_t)d_arena & 3) || ((uintptr_t)d_error & 3)) {
+        ytgb_set_error("ytgb_vertex_bricks: null or misaligned device array");
+        return YTGB_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    vertex_bricks_kernel<<<n_bricks, PREP_BLOCK, 0, s>>>(d_cells, n_cells, d_grid_offset, d_grid_dims, n_grids,
+                                                          d_brick_grid, d_brick_lo, d_bricks, field, log_field,
+                                                          d_arena, arena_len, d_error);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_vertex_bricks: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    return YTGB_OK;
+}

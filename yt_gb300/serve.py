@@ -159,7 +159,7 @@ class RenderServer:
                 reqs = [admitted.popleft() for _ in range(min(self.max_batch, len(admitted)))]
                 inflight.append(self._launch(reqs, free.pop(), now))
                 continue
-            if not admitted and inflight and (not pending or pending[0].arrival > now):
+            if not admitted and (not pending or pending[0].arrival > now):
                 # nothing to launch: wait briefly for arrivals or completions
                 nxt = pending[0].arrival - now if pending else 1e-3
                 time.sleep(max(0.0, min(nxt, 2e-4)))

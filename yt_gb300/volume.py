@@ -60,7 +60,6 @@ class BrickSet:
         n = len(bricks)
         self.n = n
         m = max(n, 1)
-        desc = np.zeros(m, dtype=BRICK_DTYPE)
         f64 = np.dtype(np.float64)
         u8 = np.dtype(np.uint8)
         dims_l, le_l, re_l, nf_l = [], [], [], []
@@ -115,6 +114,81 @@ class BrickSet:
         fstart = np.concatenate([[0], np.cumsum(nfields[:n])]).astype(np.int64)
         sizes_min = np.minimum.reduceat(fsize, fstart[:-1]) if n else fsize
         sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
+        desc, stride, data_off, total, bounds = self._layout(dims, le, re, nfields, sizes_min, sizes_max)
+        buf = _pinned((max(total, 4),), torch.float32, self.device)
+        L = _lib.lib()
+        # float64 -> float32 gather into the pinned arena, on all host cores
+        src = np.array(fptr, dtype=np.uintp)
+        fbrick = np.repeat(np.arange(n), nfields[:n])
+        dst_f = (data_off[fbrick] + (np.arange(len(fptr)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
+        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
+                                      buf.data_ptr(), 0), "ytgb_pack_fields")
+        # masks: kept only when some cell is masked out
+        mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
+        desc["mask_offset"][:] = -1
+        mbuf = None
+        if mk_k:
+            msrc = np.array(mptr, dtype=np.uintp)
+            mcnt = mk_size
+            mdst = mstart[mk_brick]
+            ones = C.c_int32()
+            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k), None, 0,
+                                         C.byref(ones)), "ytgb_pack_masks")
+            if not ones.value:
+                mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
+                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k),
+                                             mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
+                desc["mask_offset"][mk_brick] = mdst
+        self.desc_host = desc
+        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
+        self.data = buf.to(self.device, non_blocking=True)
+        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
+        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
+        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
+        self.nbytes = int(self.data.numel() * 4)
+        self.upload_bytes = int(self.data.numel() * 4 + self.bounds.numel() * 8 + self.desc.numel() +
+                                (self.masks.numel() if self.masks is not None else 0))
+
+    @classmethod
+    def on_device(cls, dims, le, re, device="cuda", n_fields=1):
+        """Bricks of the given geometry whose vertex-centred fields are
+        written on the device (``AMRKDTree.device_brickset``): descriptors and
+        boundary tables as usual, a float32 arena of (dims+1)^3 values per
+        field allocated on the device and left unfilled, no masks."""
+        self = cls.__new__(cls)
+        self.device = torch.device(device)
+        d = np.ascontiguousarray(dims, dtype=np.int64).reshape(-1, 3)
+        n = d.shape[0]
+        self.n = n
+        m = max(n, 1)
+        if n and (d <= 0).any():
+            raise ValueError("brick dims must be positive")
+        dims_m = np.ones((m, 3), dtype=np.int64)
+        le_m = np.zeros((m, 3))
+        re_m = np.ones((m, 3))
+        dims_m[:n] = d
+        le_m[:n] = np.asarray(le, dtype=np.float64).reshape(n, 3)
+        re_m[:n] = np.asarray(re, dtype=np.float64).reshape(n, 3)
+        nfields = np.zeros(m, dtype=np.int64)
+        nfields[:n] = n_fields
+        verts = (d + 1).prod(axis=1)
+        desc, stride, data_off, total, bounds = self._layout(dims_m, le_m, re_m, nfields, verts, verts)
+        desc["mask_offset"][:] = -1
+        self.desc_host = desc
+        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
+        self.data = torch.empty(max(total, 4), dtype=torch.float32, device=self.device)
+        self.masks = None
+        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
+        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
+        self.nbytes = int(self.data.numel() * 4)
+        self.upload_bytes = int(self.bounds.numel() * 8 + self.desc.numel())
+        return self
+
+    def _layout(self, dims, le, re, nfields, sizes_min, sizes_max):
+        """Descriptors, arena strides/offsets and cell-boundary tables of
+        bricks with the given geometry and per-field element counts."""
+        n, m = self.n, max(self.n, 1)
+        desc = np.zeros(m, dtype=BRICK_DTYPE)
         self.cells = dims.prod(axis=1)
         self.verts = (dims + 1).prod(axis=1)
         self.min_elems = np.zeros(m, dtype=np.int64)
@@ -150,39 +224,7 @@ class BrickSet:
         desc["bounds_offset"][:n] = starts[:-1].reshape(n, 3)[:, 0] if n else []
         if nb_total == 0:
             bounds = np.zeros(1)
-        buf = _pinned((max(total, 4),), torch.float32, self.device)
-        L = _lib.lib()
-        # float64 -> float32 gather into the pinned arena, on all host cores
-        src = np.array(fptr, dtype=np.uintp)
-        fbrick = np.repeat(np.arange(n), nfields[:n])
-        dst_f = (data_off[fbrick] + (np.arange(len(fptr)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
-        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
-                                      buf.data_ptr(), 0), "ytgb_pack_fields")
-        # masks: kept only when some cell is masked out
-        mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
-        desc["mask_offset"][:] = -1
-        mbuf = None
-        if mk_k:
-            msrc = np.array(mptr, dtype=np.uintp)
-            mcnt = mk_size
-            mdst = mstart[mk_brick]
-            ones = C.c_int32()
-            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k), None, 0,
-                                         C.byref(ones)), "ytgb_pack_masks")
-            if not ones.value:
-                mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
-                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k),
-                                             mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
-                desc["mask_offset"][mk_brick] = mdst
-        self.desc_host = desc
-        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
-        self.data = buf.to(self.device, non_blocking=True)
-        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
-        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
-        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
-        self.nbytes = int(self.data.numel() * 4)
-        self.upload_bytes = int(self.data.numel() * 4 + self.bounds.numel() * 8 + self.desc.numel() +
-                                (self.masks.numel() if self.masks is not None else 0))
+        return desc, stride, data_off, total, bounds
 
     def rects(self, view: _lib.View, order: np.ndarray) -> np.ndarray:
         """Per-order-entry pixel rectangles (ytgb_brick_rects)."""
