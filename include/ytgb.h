@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define YTGB_ABI_VERSION 1
+#define YTGB_ABI_VERSION 2
 
 #define YTGB_OK 0
 #define YTGB_ERR_INVALID (-1)   /* bad argument, detected on the host */
@@ -26,12 +26,14 @@ extern "C" {
 #define YTGB_ERR_DEVICE (-3)    /* a device-side guard tripped (see error word) */
 
 /* sampler kinds: VolumeRenderSampler (image_samplers.pyx:405-487),
- * ProjectionSampler (:327-343), InterpolatedProjectionSampler (:346-403) and
- * the MIP sampler (ProjectionSampler with max; no reference counterpart). */
+ * ProjectionSampler (:327-343), InterpolatedProjectionSampler (:346-403),
+ * the MIP sampler (ProjectionSampler with max; no reference counterpart) and
+ * LightSourceRenderSampler (:496-590). */
 #define YTGB_VOLUME_RENDER 0
 #define YTGB_PROJECTION 1
 #define YTGB_INTERPOLATED_PROJECTION 2
 #define YTGB_MIP 3
+#define YTGB_LIGHT_SOURCE 4
 
 /* ray generation: generate_vector_info_plane_parallel (lenses.pyx:179-192);
  * generate_vector_info_null, i.e. per-pixel arrays (lenses.pyx:196-207); or
@@ -122,7 +124,7 @@ typedef struct ytgb_tf {
 /* Arguments of one render: cast_through_kdtree (image_samplers.pyx:146-197)
  * for every brick of `order`, in that order, in one launch. */
 typedef struct ytgb_render_args {
-    int32_t kind;              /* YTGB_VOLUME_RENDER ... YTGB_MIP */
+    int32_t kind;              /* YTGB_VOLUME_RENDER ... YTGB_LIGHT_SOURCE */
     int32_t n_samples;         /* samples per cell (VR / interpolated projection) */
     int32_t n_order;           /* number of entries in order / rects */
     uint32_t flags;            /* YTGB_FLAG_* */
@@ -133,13 +135,19 @@ typedef struct ytgb_render_args {
     const float *data;         /* device float32 arena */
     const uint8_t *masks;      /* device mask arena, or NULL when all are -1 */
     const double *bounds;      /* device cell-boundary tables (see ytgb_brick) */
-    ytgb_tf tf;                /* by value, from ytgb_tf_pack (VR only) */
-    const float *tf_tables;    /* device, VR only */
+    ytgb_tf tf;                /* by value, from ytgb_tf_pack (VR and light source) */
+    const float *tf_tables;    /* device, VR and light source */
     double *image;             /* device (nx,ny,4) float64, updated in place */
     const double *zbuffer;     /* device (nx,ny) float64, or NULL (all ones) */
     unsigned long long *counters; /* device [4]: cell visits, ray-brick walks, rays, cells
                                   * outside their brick (skipped); or NULL */
     int32_t *error;            /* device error word (0 = ok), or NULL */
+    /* LightSourceRenderSampler only (image_samplers.pyx:496-590) */
+    const float *data_lo;      /* device: data - (float)data for every arena value (the
+                                * gradient's differences), or NULL (taken as 0) */
+    float light_dir[3];        /* normalised light direction */
+    float light_rgba[4];
+    int32_t pad_light;
 } ytgb_render_args;
 
 /* One view of a multi-view batch (device memory), as filled by
@@ -233,11 +241,13 @@ int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int3
  * brick b takes grid d_brick_grid[b] from vertex d_brick_lo[3b..] with the
  * dims and arena slot of d_bricks[b].  Every index is checked on the device;
  * a brick that does not fit is skipped and YTGB_DEVERR_BAD_BRICK is written
- * to *d_error (read it with ytgb_check_error). */
+ * to *d_error (read it with ytgb_check_error).  d_arena_lo (or NULL) receives
+ * each value's float32 rounding error, laid out like d_arena. */
 int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const int64_t *d_grid_offset,
                        const int32_t *d_grid_dims, int32_t n_grids, const int32_t *d_brick_grid,
                        const int32_t *d_brick_lo, const ytgb_brick *d_bricks, int32_t n_bricks, int32_t field,
-                       int32_t log_field, float *d_arena, int64_t arena_len, int32_t *d_error, void *stream);
+                       int32_t log_field, float *d_arena, int64_t arena_len, int32_t *d_error, void *stream,
+                       float *d_arena_lo);
 
 /* ---- host: brick marshalling -------------------------------------------- */
 /* No reference counterpart: yt's sampler reads each PartitionedGrid's
@@ -248,6 +258,11 @@ int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const int64_t *d_
  * Round to nearest even, as numpy's astype(float32). */
 int ytgb_pack_fields(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
                      float *dst, int32_t n_threads);
+/* The same gather writing each value's float32 part to dst_hi and its
+ * float32 rounding error (value - hi, rounded to float32; 0 for non-finite
+ * values) to dst_lo: the low parts the light-source sampler's gradient uses. */
+int ytgb_pack_fields_split(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
+                           float *dst_hi, float *dst_lo, int32_t n_threads);
 /* The same gather for uint8 cell masks (dst may be NULL: check only);
  * *all_ones = 1 when every mask byte is 1 (VolumeRenderSampler then needs no
  * mask, image_samplers.pyx:461-462). */

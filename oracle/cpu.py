@@ -19,8 +19,9 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libytoracle.so"
 
-VR, PROJ, IPROJ, MIP = 0, 1, 2, 3
-KIND_BY_NAME = {"volume_render": VR, "projection": PROJ, "interpolated_projection": IPROJ, "mip": MIP}
+VR, PROJ, IPROJ, MIP, LIGHT = 0, 1, 2, 3, 4
+KIND_BY_NAME = {"volume_render": VR, "projection": PROJ, "interpolated_projection": IPROJ, "mip": MIP,
+                "light_source": LIGHT}
 
 _dp = C.POINTER(C.c_double)
 
@@ -76,6 +77,8 @@ class YoSampler(C.Structure):
         ("image", _dp),
         ("zbuffer", _dp),
         ("fits", YoFit * 6),
+        ("light_dir", C.c_double * 3),
+        ("light_rgba", C.c_double * 4),
     ]
 
 
@@ -165,7 +168,8 @@ class OracleSampler:
     place, like the reference's ``aimage``."""
 
     def __init__(self, kind, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width,
-                 lens_type="plane-parallel", camera_data=None, zbuffer=None, n_samples=1, tf=None):
+                 lens_type="plane-parallel", camera_data=None, zbuffer=None, n_samples=1, tf=None,
+                 light_dir=(1.0, 1.0, 1.0), light_rgba=(1.0, 1.0, 1.0, 1.0)):
         s = YoSampler()
         self._keep = []
         self.image = image
@@ -221,6 +225,13 @@ class OracleSampler:
                               int(tf.weight_field_ids[i]), int(tf.weight_table_ids[i]), _ptr(d0), _ptr(dy))
             for i in range(6):
                 s.field_table_ids[i] = int(tf.field_table_ids[i])
+        # LightSourceRenderSampler.__cinit__ (image_samplers.pyx:530-536)
+        ld = np.asarray(light_dir, dtype=np.float64)
+        ld = ld / np.sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2])
+        for i in range(3):
+            s.light_dir[i] = float(ld[i])
+        for i in range(4):
+            s.light_rgba[i] = float(light_rgba[i])
         self.s = s
 
     def render(self, bricks: OracleBricks, order=None, num_threads=0) -> int:

@@ -378,13 +378,15 @@ def brick_data(node, grid, vertex_data):
     return data, mask, nle.copy(), nre.copy(), dims.astype("int64")
 
 
-def render(kind, cam: Camera, bricks, order, tf=None, n_samples=1, num_threads=0, zbuffer=None):
+def render(kind, cam: Camera, bricks, order, tf=None, n_samples=1, num_threads=0, zbuffer=None,
+           light_dir=(1.0, 1.0, 1.0), light_rgba=(1.0, 1.0, 1.0, 1.0)):
     """KDTreeVolumeSource.render's brick loop on the C oracle; returns the raw
     sampler image (before finalize_image) and the visited-cell count."""
     p = cam.sampler_params()
     s = cpu.OracleSampler(kind, p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"],
                           p["x_vec"], p["y_vec"], p["width"], lens_type=p["lens_type"],
-                          camera_data=p["camera_data"], zbuffer=zbuffer, n_samples=n_samples, tf=tf)
+                          camera_data=p["camera_data"], zbuffer=zbuffer, n_samples=n_samples, tf=tf,
+                          light_dir=light_dir, light_rgba=light_rgba)
     ob = bricks if isinstance(bricks, cpu.OracleBricks) else cpu.OracleBricks(bricks)
     visits = s.render(ob, order, num_threads=num_threads)
     return p["image"], visits

@@ -42,6 +42,7 @@
 #define YO_PROJ 1
 #define YO_IPROJ 2
 #define YO_MIP 3
+#define YO_LIGHT 4
 
 typedef struct {
     double left_edge[3];
@@ -84,6 +85,8 @@ typedef struct {
     double *image;          /* nx*ny*4 */
     const double *zbuffer;  /* nx*ny */
     yo_fit fits[6];
+    double light_dir[3];   /* LightSourceRenderSampler: normalised */
+    double light_rgba[4];
 } yo_sampler;
 
 /* fp_utils.pxd helpers: first-argument-wins semantics */
@@ -349,6 +352,90 @@ static void sample_interp_proj(const yo_vc *vc, const double v_pos[3], const dou
     }
 }
 
+/* eval_gradient (fixed_interpolator.cpp:116-148): one-sided or central
+ * differences of offset_interpolate, 0.05 apart, normalised to -grad/|grad|. */
+static void yo_eval_gradient(const int ds[3], double dp[3], const double *data, double *grad)
+{
+    int i;
+    double denom, plus, minus, backup, normval = 0.0;
+    for (i = 0; i < 3; i++) {
+        backup = dp[i];
+        grad[i] = 0.0;
+        if (dp[i] >= 0.95) { plus = dp[i]; minus = dp[i] - 0.05; }
+        else if (dp[i] <= 0.05) { plus = dp[i] + 0.05; minus = 0.0; }
+        else { plus = dp[i] + 0.05; minus = dp[i] - 0.05; }
+        denom = plus - minus;
+        dp[i] = plus;
+        grad[i] += yo_offset_interpolate(ds, dp, data) / denom;
+        dp[i] = minus;
+        grad[i] -= yo_offset_interpolate(ds, dp, data) / denom;
+        dp[i] = backup;
+        normval += grad[i] * grad[i];
+    }
+    if (normval != 0.0) {
+        normval = sqrt(normval);
+        for (i = 0; i < 3; i++) grad[i] /= -normval;
+    } else {
+        grad[0] = grad[1] = grad[2] = 0.0;
+    }
+}
+
+/* FIT_eval_transfer_with_light (field_interpolation_tables.pxd:115-143) */
+static inline void fit_eval_transfer_with_light(double dt, const double *dvs, const double *grad,
+                                                const double *l_dir, const double *l_rgba, double *rgba,
+                                                int n_fits, const yo_fit fits[6], const int field_table_ids[6],
+                                                int grey_opacity)
+{
+    int i, fid;
+    double ta, dot_prod = 0.0;
+    double istorage[6] = {0, 0, 0, 0, 0, 0};
+    double trgba[6];
+    for (i = 0; i < 3; i++) dot_prod += l_dir[i] * grad[i];
+    for (i = 0; i < n_fits; i++) istorage[i] = fit_get(&fits[i], dvs);
+    for (i = 0; i < n_fits; i++) {
+        fid = fits[i].weight_table_id;
+        if (fid != -1) istorage[i] *= istorage[fid];
+    }
+    for (i = 0; i < 6; i++) trgba[i] = istorage[field_table_ids[i]];
+    if (grey_opacity == 1) {
+        ta = yo_fmax(1.0 - dt * (trgba[0] + trgba[1] + trgba[2]), 0.0);
+        for (i = 0; i < 3; i++) rgba[i] = (1. - ta) * trgba[i] * (1. + dot_prod * l_rgba[i]) + ta * rgba[i];
+    } else {
+        for (i = 0; i < 3; i++) {
+            ta = yo_fmax(1.0 - dt * trgba[i], 0.0);
+            rgba[i] = (1. - ta) * trgba[i] * (1. + dot_prod * l_rgba[i]) + ta * rgba[i];
+        }
+    }
+}
+
+/* LightSourceRenderSampler.sample (image_samplers.pyx:551-590): like
+ * VolumeRenderSampler.sample without the mask test, with a gradient of
+ * field 0 at every sample. */
+static void sample_light(const yo_vc *vc, const double v_pos[3], const double v_dir[3],
+                         double enter_t, double exit_t, const int index[3], void *data)
+{
+    yo_acc *im = (yo_acc *)data;
+    const yo_sampler *s = im->s;
+    int i, j, k;
+    int offset = index[0] * (vc->dims[1] + 1) * (vc->dims[2] + 1) + index[1] * (vc->dims[2] + 1) + index[2];
+    double dp[3], ds[3], dvs[6] = {0, 0, 0, 0, 0, 0}, grad[3];
+    double dt = (exit_t - enter_t) / s->n_samples;
+    if (!yo_inside(vc, index)) return;
+    for (i = 0; i < 3; i++) {
+        dp[i] = (enter_t + 0.5 * dt) * v_dir[i] + v_pos[i];
+        dp[i] -= index[i] * vc->dds[i] + vc->left_edge[i];
+        dp[i] *= vc->idds[i];
+        ds[i] = v_dir[i] * vc->idds[i] * dt;
+    }
+    for (k = 0; k < s->n_samples; k++) {
+        for (j = 0; j < vc->n_fields; j++) dvs[j] = yo_offset_interpolate(vc->dims, dp, vc->data[j] + offset);
+        yo_eval_gradient(vc->dims, dp, vc->data[0] + offset, grad);
+        fit_eval_transfer_with_light(dt, dvs, grad, s->light_dir, s->light_rgba, im->rgba, s->n_fits, s->fits,
+                                     s->field_table_ids, s->grey_opacity);
+        for (j = 0; j < 3; j++) dp[j] += ds[j];
+    }
+}
+
 static void extent_plane_parallel(const yo_sampler *im, const yo_vc *vc, int64_t rv[4])
 {
     double temp, cx, cy, extrema[4];
@@ -487,6 +574,7 @@ static yo_sample_fn pick_sampler(int kind)
     case YO_VR: return sample_vr;
     case YO_PROJ: return sample_projection;
     case YO_IPROJ: return sample_interp_proj;
+    case YO_LIGHT: return sample_light;
     default: return sample_mip;
     }
 }

@@ -17,6 +17,8 @@ tests do not depend on the synthetic generators staying bit-stable.
 * vr.npz        VolumeRenderSampler images: a 16^3 blob brick, 4-layer CTF,
                 three cameras (axis-aligned and oblique plane-parallel,
                 perspective), n_samples 1 and 3
+* light.npz     LightSourceRenderSampler images on the vr.npz brick: three
+                cameras x two lights (n_samples 1 and 3) x grey opacity {0,1}
 * proj.npz      ProjectionSampler (cell-centred) and
                 InterpolatedProjectionSampler (vertex-centred) images
 * kd.npz        AMRKDTree leaves and viewpoint orders (amr_kdtools.pyx
@@ -122,6 +124,38 @@ def vr():
     np.savez_compressed(HERE / "vr.npz", **out)
 
 
+LIGHTS = [((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0)), ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0))]
+
+
+def light():
+    """LightSourceRenderSampler (image_samplers.pyx:496-590): the vr.npz brick
+    and three cameras, two lights (the first at n_samples 1, the second at
+    3), each with and without grey opacity."""
+    g = testing.blob_grid(16, seed=0)
+    v = np.log10(ref_vertex(g.data))
+    lg = np.log10(g.data)
+    bounds = (float(lg.min()), float(lg.max()))
+    layers = testing.ctf_layers(bounds, 4)
+    tf = glue.color_tf_from_layers(bounds, 64, layers)
+    tfg = glue.color_tf_from_layers(bounds, 64, layers)
+    tfg.grey_opacity = 1
+    out = {"vertex": v, "tf_y": np.array([t.y for t in tf.tables]), "tf_bounds": np.array(bounds)}
+    dims = np.array([16, 16, 16], dtype=np.int64)
+    for ci, (pos, width, res, lens) in enumerate(CAMS):
+        for li, (ldir, lrgba) in enumerate(LIGHTS):
+            for ns in ((1,) if li == 0 else (3,)):
+                for grey, t in ((0, tf), (1, tfg)):
+                    cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+                    p = cam.sampler_params()
+                    s = RIS.LightSourceRenderSampler(*sampler_args(p), t, ns, light_dir=np.array(ldir),
+                                                     light_rgba=np.array(lrgba), lens_type=p["lens_type"],
+                                                     camera_data=p["camera_data"], zbuffer=np.ones(res))
+                    s(PartitionedGrid(0, [v], np.ones((16, 16, 16), "uint8"), np.zeros(3), np.ones(3), dims),
+                      num_threads=1)
+                    out[f"img_{ci}_{li}_{ns}_{grey}"] = np.array(s.aimage)
+    np.savez_compressed(HERE / "light.npz", **out)
+
+
 def proj():
     rng = np.random.default_rng(13)
     cell = np.exp(rng.standard_normal((12, 12, 12)))
@@ -201,6 +235,7 @@ if __name__ == "__main__":
     gz()
     trace()
     vr()
+    light()
     proj()
     kd_and_amr()
     for f in sorted(HERE.glob("*.npz")):

@@ -14,7 +14,7 @@ using namespace ytgb;
 template <int MODE, int CTF>
 static void run(const ytgb_render_args &a, unsigned long long *hashes, long long *counts, unsigned long long *cnt) {
     std::vector<float4> tab;
-    if (MODE == MODE_VR) {
+    if (MODE == MODE_VR || MODE == MODE_LIGHT) {
         const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
         int nb = a.tf.nbins_max;
         if (CTF) {
@@ -57,6 +57,7 @@ extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long lo
     case YTGB_VOLUME_RENDER: if (a->tf.ctf_fast) run<MODE_VR, 1>(*a, 0, 0, cnt); else run<MODE_VR, 0>(*a, 0, 0, cnt); break;
     case YTGB_PROJECTION: run<MODE_PROJ, 0>(*a, 0, 0, cnt); break;
     case YTGB_INTERPOLATED_PROJECTION: run<MODE_IPROJ, 0>(*a, 0, 0, cnt); break;
+    case YTGB_LIGHT_SOURCE: run<MODE_LIGHT, 0>(*a, 0, 0, cnt); break;
     default: run<MODE_MIP, 0>(*a, 0, 0, cnt);
     }
     return 0;

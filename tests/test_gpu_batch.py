@@ -63,16 +63,19 @@ def test_batch_every_sampler_path(cuda, blocks):
     w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
     r_ctf = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
     cases = [(r_ctf, _lib.VOLUME_RENDER, 1), (r_mv, _lib.VOLUME_RENDER, 2), (r_lin, _lib.PROJECTION, 1),
-             (r_lin, _lib.INTERPOLATED_PROJECTION, 3), (r_lin, _lib.MIP, 1)]
-    jobs = [Job(r, cam, kind, n_samples=ns) for (r, kind, ns) in cases for cam in cams(4, seed=7)]
+             (r_lin, _lib.INTERPOLATED_PROJECTION, 3), (r_lin, _lib.MIP, 1), (r_ctf, _lib.LIGHT_SOURCE, 2)]
+    light = ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0))
+    jobs = [Job(r, cam, kind, n_samples=ns, light=light if kind == _lib.LIGHT_SOURCE else None)
+            for (r, kind, ns) in cases for cam in cams(4, seed=7)]
     b = Batch(jobs, device=cuda, blocks=blocks)
-    assert len(b.groups) == 5
+    assert len(b.groups) == 6
     b.launch()
     torch.cuda.synchronize()
     b.check()
     for j in jobs:
-        alone = j.renderer.render(j.camera, kind=j.kind, n_samples=j.n_samples)
-        assert not torch.isnan(alone).any()
+        alone = j.renderer.render(j.camera, kind=j.kind, n_samples=j.n_samples, light=j.light)
+        if j.kind != _lib.LIGHT_SOURCE:
+            assert not torch.isnan(alone).any()
         assert same_bits(alone, j.image), (j.kind, j.n_samples)
 
 

@@ -12,35 +12,41 @@ from oracle import cpu as ocpu
 from yt_gb300 import _lib, testing, workloads
 from yt_gb300.camera import Camera
 from yt_gb300.render import Renderer, relative_error
+from yt_gb300.transfer_functions import pack
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-5
 KIND_NAME = {_lib.VOLUME_RENDER: "volume_render", _lib.PROJECTION: "projection",
-             _lib.INTERPOLATED_PROJECTION: "interpolated_projection", _lib.MIP: "mip"}
+             _lib.INTERPOLATED_PROJECTION: "interpolated_projection", _lib.MIP: "mip",
+             _lib.LIGHT_SOURCE: "light_source"}
 
 
-def oracle_render(bricks, cam, order, kind, tf=None, n_samples=1, zbuffer=None, image=None):
+def oracle_render(bricks, cam, order, kind, tf=None, n_samples=1, zbuffer=None, image=None, light=None):
     p = cam.sampler_params()
     img = p["image"] if image is None else image.copy()
+    ld, lrgba = light if light is not None else ((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0))
     s = ocpu.OracleSampler(KIND_NAME[kind], p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], img,
                            p["x_vec"], p["y_vec"], p["width"], lens_type=p["lens_type"],
-                           camera_data=p["camera_data"], zbuffer=zbuffer, n_samples=n_samples, tf=tf)
+                           camera_data=p["camera_data"], zbuffer=zbuffer, n_samples=n_samples, tf=tf,
+                           light_dir=ld, light_rgba=lrgba)
     ob = ocpu.OracleBricks(bricks)
     visits = s.render(ob, order)
     h, c = s.trace(ob, order)
     return img, visits, h, c
 
 
-def check_view(r: Renderer, bricks, cam, kind, tf=None, n_samples=1, channels=(0, 1, 2), zbuffer=None):
+def check_view(r: Renderer, bricks, cam, kind, tf=None, n_samples=1, channels=(0, 1, 2), zbuffer=None,
+               light=None):
     import torch
 
     order = r.order(cam)
     zb = None if zbuffer is None else torch.from_numpy(zbuffer).to(r.device)
     r.counters.zero_()
-    img = r.render(cam, kind=kind, n_samples=n_samples, order=order, zbuffer=zb).cpu().numpy()
+    img = r.render(cam, kind=kind, n_samples=n_samples, order=order, zbuffer=zb, light=light).cpu().numpy()
     r.check()
-    ref, visits, h_ref, c_ref = oracle_render(bricks, cam, order, kind, tf=tf, n_samples=n_samples, zbuffer=zbuffer)
+    ref, visits, h_ref, c_ref = oracle_render(bricks, cam, order, kind, tf=tf, n_samples=n_samples, zbuffer=zbuffer,
+                                              light=light)
     mx, rms = relative_error(img, ref, channels=channels)
     assert mx <= TOL, f"max relative error {mx:.3e} (rms {rms:.3e})"
     assert int(r.counters[0].item()) == visits
@@ -168,3 +174,50 @@ def test_drop_in_sampler_api(cuda):
     mx, _ = relative_error(img, ref, channels=(0, 1, 2))
     assert mx <= TOL
     assert int(s.last_counters[0]) == visits
+
+
+LIGHTS = [((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0)), ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0))]
+
+
+@pytest.mark.parametrize("lens", ["plane-parallel", "perspective"])
+@pytest.mark.parametrize("with_lo", [False, True])
+def test_light_source(cuda, lens, with_lo):
+    """LightSourceRenderSampler: uniform brick (grey and colour opacity, two
+    lights, 1 and 3 samples) and the AMR bricks (NaN vertices from log10 of
+    extrapolated non-positive values included: NaN pixels coincide)."""
+    from yt_gb300.volume import BrickSet
+
+    w = workloads.uniform_vr(n=24, res=40)
+    cam = Camera((1.2, 0.35, -0.8), (0.5, 0.5, 0.5), 1.2 if lens == "perspective" else 1.0, 40, lens_type=lens)
+    r = Renderer(BrickSet(w.bricks, device=cuda, with_lo=with_lo), w.tf, device=cuda, kdtree=w.kdtree)
+    for grey in (False, True):
+        w.tf.grey_opacity = grey
+        r.packed = pack(w.tf)
+        for light in LIGHTS:
+            for ns in (1, 3):
+                check_view(r, w.bricks, cam, _lib.LIGHT_SOURCE, tf=w.tf, n_samples=ns, light=light)
+    w.tf.grey_opacity = False
+    a = workloads.amr_vr(root=32, levels=2, patch=8, res=48)
+    ra = Renderer(BrickSet(a.bricks, device=cuda, with_lo=with_lo), a.tf, device=cuda, kdtree=a.kdtree)
+    check_view(ra, a.bricks, a.views[0].camera, _lib.LIGHT_SOURCE, tf=a.tf, light=LIGHTS[1])
+
+
+def test_light_source_drop_in(cuda):
+    """The LightSourceRenderSampler class driven like yt drives its sampler."""
+    from yt_gb300.image_samplers import LightSourceRenderSampler
+    from yt_gb300.partitioned_grid import PartitionedGrid
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
+    cam = w.views[0].camera
+    p = cam.sampler_params()
+    order = w.order(cam)
+    s = LightSourceRenderSampler(np.atleast_3d(p["vp_pos"]), np.atleast_3d(p["vp_dir"]), p["center"], p["bounds"],
+                                 p["image"], p["x_vec"], p["y_vec"], p["width"], "KDTree", w.tf, 2,
+                                 light_dir=np.array([0.2, -1.0, 0.5]), light_rgba=np.array([1.0, 0.8, 0.6, 1.0]),
+                                 lens_type=p["lens_type"], camera_data=p["camera_data"])
+    for k in order:
+        s(PartitionedGrid(0, *w.bricks[k]), num_threads=0)
+    img = s.aimage
+    ref, *_ = oracle_render(w.bricks, cam, order, _lib.LIGHT_SOURCE, tf=w.tf, n_samples=2,
+                            light=((0.2, -1.0, 0.5), (1.0, 0.8, 0.6, 1.0)))
+    assert relative_error(img, ref, channels=(0, 1, 2))[0] <= TOL

@@ -81,6 +81,6 @@ def test_device_bricks_reject_bad_slices(cuda):
     st = L.ytgb_vertex_bricks(cells.data_ptr(), cells.numel(), goff.data_ptr(), meta.data_ptr(), 1,
                               meta.data_ptr() + 12, meta.data_ptr() + 4 * (3 + len(lg)), bs.desc.data_ptr(),
                               len(lg), 0, 0, bs.data.data_ptr(), bs.data.numel(), err.data_ptr(),
-                              C.c_void_p(s.cuda_stream))
+                              C.c_void_p(s.cuda_stream), None)
     assert st == _lib.OK
     assert L.ytgb_check_error(err.data_ptr(), C.c_void_p(s.cuda_stream)) == _lib.ERR_DEVICE

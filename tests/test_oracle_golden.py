@@ -143,3 +143,27 @@ def test_amr_volume_render_exact():
         bricks.append(glue.brick_data(node, gr, vcd[gr.id]))
     img, _ = glue.render("volume_render", cam, bricks, None, tf=tf)
     assert np.array_equal(img, g["image"])
+
+
+LIGHTS = [((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0), 1), ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0), 3)]
+
+
+@pytest.mark.parametrize("ci", range(3))
+@pytest.mark.parametrize("li", range(2))
+@pytest.mark.parametrize("grey", [0, 1])
+def test_light_source_exact(ci, li, grey):
+    """LightSourceRenderSampler (image_samplers.pyx:496-590, eval_gradient
+    fixed_interpolator.cpp:116-148, FIT_eval_transfer_with_light
+    field_interpolation_tables.pxd:115-143): oracle == compiled reference,
+    bit for bit."""
+    f = load("light.npz")
+    tf = GoldenTF(f["tf_bounds"], f["tf_y"])
+    tf.grey_opacity = grey
+    pos, width, res, lens = CAMS[ci]
+    ldir, lrgba, ns = LIGHTS[li]
+    cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+    brick = ([f["vertex"]], None, np.zeros(3), np.ones(3), [16, 16, 16])
+    img, visits = glue.render("light_source", cam, [brick], None, tf=tf, n_samples=ns, light_dir=ldir,
+                              light_rgba=lrgba)
+    assert visits > 0
+    assert np.array_equal(img, f[f"img_{ci}_{li}_{ns}_{grey}"])

@@ -14,7 +14,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libytgb.so"
 
 OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE = 0, -1, -2, -3
-VOLUME_RENDER, PROJECTION, INTERPOLATED_PROJECTION, MIP = 0, 1, 2, 3
+VOLUME_RENDER, PROJECTION, INTERPOLATED_PROJECTION, MIP, LIGHT_SOURCE = 0, 1, 2, 3, 4
 LENS_PLANE_PARALLEL, LENS_PER_PIXEL, LENS_PERSPECTIVE = 0, 1, 2
 EXTENT_PLANE_PARALLEL, EXTENT_PERSPECTIVE, EXTENT_NULL = 0, 1, 2
 FLAG_NO_COMPENSATION = 1
@@ -104,6 +104,10 @@ class RenderArgs(C.Structure):
         ("zbuffer", C.c_void_p),
         ("counters", C.c_void_p),
         ("error", C.c_void_p),
+        ("data_lo", C.c_void_p),
+        ("light_dir", C.c_float * 3),
+        ("light_rgba", C.c_float * 4),
+        ("pad_light", C.c_int32),
     ]
 
 
@@ -144,7 +148,9 @@ SIGNATURES = {
                                             C.c_int32, C.c_int32, C.c_void_p]),
     "ytgb_vertex_bricks": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
-                                     C.c_int64, C.c_void_p, C.c_void_p]),
+                                     C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_pack_fields_split": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_int32]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                   C.POINTER(C.c_int32)]),
@@ -176,7 +182,7 @@ def lib() -> C.CDLL:
                 fn = getattr(L, name)
                 fn.restype = res
                 fn.argtypes = args
-            if L.ytgb_abi_version() != 1:
+            if L.ytgb_abi_version() != 2:
                 raise YtgbError("libytgb ABI version mismatch")
             _lib = L
     return _lib

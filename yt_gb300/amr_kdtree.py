@@ -144,7 +144,7 @@ class AMRKDTree:
         ri = np.rint((self.leaf_re - gle) / dds).astype("int32")
         return lg, li, (ri - li).astype(np.int64)
 
-    def device_brickset(self, device="cuda", stream=None):
+    def device_brickset(self, device="cuda", stream=None, with_lo=False):
         """The bricks as a :class:`~yt_gb300.volume.BrickSet` prepared on the
         device: the grids' cell data is uploaded once and every leaf's
         vertex-centred (and log10'd) slice is computed there
@@ -152,7 +152,8 @@ class AMRKDTree:
         The vertex values are bit-identical to the host path's; with
         ``log_field`` the device log10 may differ from numpy's in the last
         float64 bit, which reaches the float32 brick value only when it sits
-        on a float32 rounding boundary."""
+        on a float32 rounding boundary.  ``with_lo`` also fills the values'
+        float32 rounding errors (the light-source sampler's gradient)."""
         import torch
 
         from .volume import BrickSet, _pinned
@@ -164,7 +165,7 @@ class AMRKDTree:
             raise ValueError("device brick preparation needs grids of at least 2 cells per axis")
         if (li < 0).any() or (li + dims > gshape[lg]).any():
             raise ValueError("a kd leaf does not lie inside its grid")
-        bs = BrickSet.on_device(dims, self.leaf_le, self.leaf_re, dev)
+        bs = BrickSet.on_device(dims, self.leaf_le, self.leaf_re, dev, with_lo=with_lo)
         gsize = gshape.prod(axis=1)
         goff = np.concatenate([[0], np.cumsum(gsize)]).astype(np.int64)
         host = _pinned((max(int(goff[-1]), 1),), torch.float64, dev)
@@ -183,7 +184,9 @@ class AMRKDTree:
         _lib.check(L.ytgb_vertex_bricks(cells.data_ptr(), int(goff[-1]), meta_i64.data_ptr(), base, ng,
                                         base + 4 * 3 * ng, base + 4 * (3 * ng + nb), bs.desc.data_ptr(), nb, 0,
                                         int(bool(self.log_field)), bs.data.data_ptr(), bs.data.numel(),
-                                        error.data_ptr(), C.c_void_p(s.cuda_stream)), "ytgb_vertex_bricks")
+                                        error.data_ptr(), C.c_void_p(s.cuda_stream),
+                                        bs.data_lo.data_ptr() if bs.data_lo is not None else None),
+                   "ytgb_vertex_bricks")
         _lib.check(L.ytgb_check_error(error.data_ptr(), s.cuda_stream), "ytgb_vertex_bricks")
         self.device_upload_bytes = int(cells.numel() * 8 + meta_i64.numel() * 8 + meta_i32.numel() * 4 +
                                        bs.upload_bytes)

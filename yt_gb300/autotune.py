@@ -27,7 +27,8 @@ from . import _lib
 TABLE = Path(__file__).resolve().parent / "tuning.json"
 SHAPES = (0, 1, 2)
 _SAMPLER = {_lib.VOLUME_RENDER: "vr", _lib.PROJECTION: "projection",
-            _lib.INTERPOLATED_PROJECTION: "interpolated_projection", _lib.MIP: "mip"}
+            _lib.INTERPOLATED_PROJECTION: "interpolated_projection", _lib.MIP: "mip",
+            _lib.LIGHT_SOURCE: "light_source"}
 _LENS = {_lib.LENS_PLANE_PARALLEL: "plane-parallel", _lib.LENS_PERSPECTIVE: "perspective",
          _lib.LENS_PER_PIXEL: "per-pixel"}
 _cache = None

@@ -23,6 +23,7 @@ import torch
 from . import _lib
 from .autotune import tile_shape_for
 from .render import Renderer
+from .volume import check_inputs, set_light
 
 
 @dataclass
@@ -34,6 +35,7 @@ class Job:
     image: torch.Tensor | None = None
     order: np.ndarray | None = None
     flags: int = 0
+    light: tuple | None = None   # (light_dir, light_rgba) for the light-source sampler
 
 
 @dataclass
@@ -79,7 +81,6 @@ class Batch:
             order = j.order if j.order is not None else j.renderer.order(j.camera)
             order = np.ascontiguousarray(order, dtype=np.int32)
             rects = j.renderer.bricks.rects(view, order)
-            from .volume import check_inputs
 
             check_inputs(j.renderer.bricks, view, order, j.kind, j.image)
             # rects are read as 16-byte int4: every view's table starts on a
@@ -92,10 +93,11 @@ class Batch:
         self.tables = torch.from_numpy(np.concatenate(tables)).to(self.device)
         base = self.tables.data_ptr()
         for j, (view, n_order), off in zip(self.jobs, views, offs[:-1]):
-            tf = j.renderer.packed if j.kind == _lib.VOLUME_RENDER else None
-            if j.kind == _lib.VOLUME_RENDER and tf is None:
+            uses_tf = j.kind in (_lib.VOLUME_RENDER, _lib.LIGHT_SOURCE)
+            tf = j.renderer.packed if uses_tf else None
+            if uses_tf and tf is None:
                 raise ValueError("volume rendering needs a transfer function")
-            ctf = int(tf.header.ctf_fast) if tf is not None else 0
+            ctf = int(tf.header.ctf_fast) if (tf is not None and j.kind == _lib.VOLUME_RENDER) else 0
             g = groups.setdefault((j.kind, ctf), _Group(j.kind, ctf))
             a = _lib.RenderArgs()
             a.kind = j.kind
@@ -113,6 +115,8 @@ class Batch:
                 a.tf = tf.header
                 a.tf_tables = tf.device_tables(self.device).data_ptr()
             a.image = j.image.data_ptr()
+            if j.kind == _lib.LIGHT_SOURCE:
+                set_light(a, j.renderer.bricks, j.light)
             a.counters = self.counters.data_ptr()
             a.error = self.error.data_ptr()
             g.jobs.append(a)

@@ -101,6 +101,33 @@ extern "C" int ytgb_pack_fields(const double *const *src, const int64_t *count, 
     return YTGB_OK;
 }
 
+extern "C" int ytgb_pack_fields_split(const double *const *src, const int64_t *count, const int64_t *dst_offset,
+                                      int64_t n, float *dst_hi, float *dst_lo, int32_t n_threads) {
+    std::vector<int64_t> start;
+    if (int st = check_lists(src, count, dst_offset, n, dst_hi, start, "ytgb_pack_fields_split")) return st;
+    if (n > 0 && !dst_lo) {
+        ytgb_set_error("ytgb_pack_fields_split: null low-part arena");
+        return YTGB_ERR_INVALID;
+    }
+    const int64_t total = start[n];
+    parallel_ranges(total, thread_count(n_threads, total * 16), [&](int64_t lo, int64_t hi) {
+        for_pieces(start, lo, hi, [&](int64_t k, int64_t a, int64_t b) {
+            const double *s = src[k];
+            float *dh = dst_hi + dst_offset[k];
+            float *dl = dst_lo + dst_offset[k];
+            for (int64_t i = a; i < b; i++) {
+                const float h = (float)s[i];
+                dh[i] = h;
+                // the float32 rounding error, itself rounded to float32
+                // (NaN and infinities carry 0)
+                const double r = s[i] - (double)h;
+                dl[i] = r == r && r - r == 0.0 ? (float)r : 0.0f;
+            }
+        });
+    });
+    return YTGB_OK;
+}
+
 extern "C" int ytgb_pack_masks(const uint8_t *const *src, const int64_t *count, const int64_t *dst_offset,
                                int64_t n, uint8_t *dst, int32_t n_threads, int32_t *all_ones) {
     std::vector<int64_t> start;

@@ -25,7 +25,8 @@ constexpr int PREP_BLOCK = 256;
 __global__ void __launch_bounds__(PREP_BLOCK)
 vertex_bricks_kernel(const double *cells, int64_t n_cells, const int64_t *grid_offset, const int32_t *grid_dims,
                      int32_t n_grids, const int32_t *brick_grid, const int32_t *brick_lo, const ytgb_brick *bricks,
-                     int32_t field, int32_t log_field, float *arena, int64_t arena_len, int32_t *error) {
+                     int32_t field, int32_t log_field, float *arena, int64_t arena_len, int32_t *error,
+                     float *arena_lo) {
     const int b = blockIdx.x;
     const int g = brick_grid[b];
     if (g < 0 || g >= n_grids) {
@@ -59,7 +60,12 @@ vertex_bricks_kernel(const double *cells, int64_t n_cells, const int64_t *grid_o
         const int i = (int)(r / e1);
         double v = vertex_value(c, n0, n1, n2, l0 + i, l1 + j, l2 + k);
         if (log_field) v = v <= 0.0 ? nan("") : log10(v);
-        out[t] = (float)v;
+        const float h = (float)v;
+        out[t] = h;
+        if (arena_lo) {
+            const double err = v - (double)h;
+            arena_lo[out0 + t] = isfinite(err) ? (float)err : 0.0f;
+        }
     }
 }
 
@@ -69,7 +75,7 @@ extern "C" int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const 
                                   const int32_t *d_grid_dims, int32_t n_grids, const int32_t *d_brick_grid,
                                   const int32_t *d_brick_lo, const ytgb_brick *d_bricks, int32_t n_bricks,
                                   int32_t field, int32_t log_field, float *d_arena, int64_t arena_len,
-                                  int32_t *d_error, void *stream) {
+                                  int32_t *d_error, void *stream, float *d_arena_lo) {
     if (n_bricks < 0 || n_grids < 0 || n_cells < 0 || arena_len < 0 || field < 0 || field > 5) {
         ytgb_set_error("ytgb_vertex_bricks: bad sizes");
         return YTGB_ERR_INVALID;
@@ -78,14 +84,14 @@ extern "C" int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const 
     if (!d_cells || !d_grid_offset || !d_grid_dims || !d_brick_grid || !d_brick_lo || !d_bricks || !d_arena ||
         ((uintptr_t)d_cells & 7) || ((uintptr_t)d_grid_offset & 7) || ((uintptr_t)d_grid_dims & 3) ||
         ((uintptr_t)d_brick_grid & 3) || ((uintptr_t)d_brick_lo & 3) || ((uintptr_t)d_bricks & 7) ||
-        ((uintptr_t)d_arena & 3) || ((uintptr_t)d_error & 3)) {
+        ((uintptr_t)d_arena & 3) || ((uintptr_t)d_error & 3) || ((uintptr_t)d_arena_lo & 3)) {
         ytgb_set_error("ytgb_vertex_bricks: null or misaligned device array");
         return YTGB_ERR_INVALID;
     }
     cudaStream_t s = (cudaStream_t)stream;
     vertex_bricks_kernel<<<n_bricks, PREP_BLOCK, 0, s>>>(d_cells, n_cells, d_grid_offset, d_grid_dims, n_grids,
                                                           d_brick_grid, d_brick_lo, d_bricks, field, log_field,
-                                                          d_arena, arena_len, d_error);
+                                                          d_arena, arena_len, d_error, d_arena_lo);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         ytgb_set_error(std::string("ytgb_vertex_bricks: ") + cudaGetErrorString(e));

@@ -32,7 +32,8 @@ constexpr int MODE_VR = YTGB_VOLUME_RENDER;
 constexpr int MODE_PROJ = YTGB_PROJECTION;
 constexpr int MODE_IPROJ = YTGB_INTERPOLATED_PROJECTION;
 constexpr int MODE_MIP = YTGB_MIP;
-constexpr int MODE_TRACE = 4;
+constexpr int MODE_LIGHT = YTGB_LIGHT_SOURCE;
+constexpr int MODE_TRACE = 5;
 
 // ---- exact float64 arithmetic (never contracted into FMA) -----------------
 #ifdef __CUDA_ARCH__
@@ -508,6 +509,24 @@ YTGB_HD void acc_grey(float &h, float &l, float dt, float e, float da, bool comp
     }
 }
 
+// One channel of FIT_eval_transfer_with_light (field_interpolation_tables.pxd:
+// 115-143): x <- (1 - ta) e (1 + dot l) + ta x with ta = max(1 - d, 0) and
+// d = dt e (dt (e0 + e1 + e2) with grey opacity), i.e. x + d (y - x) with
+// y = e (1 + dot l) while d < 1, else y.
+YTGB_HD void acc_light(float &h, float &l, float d, float y, bool comp) {
+    if (d < 1.0f) {
+        if (comp) {
+            const float u = fsub(fsub(y, h), l);
+            acc_add(h, l, fmul(d, u));
+        } else {
+            h = ffma(d, fsub(y, h), h);
+        }
+    } else {
+        h = y;
+        l = 0.0f;
+    }
+}
+
 YTGB_HD float pick6(const float a[6], int i) {
     float r = a[0];
     r = i == 1 ? a[1] : r;
@@ -531,6 +550,53 @@ YTGB_HD float trilinear(const float *__restrict__ p, int sy, int sx, float dx, f
     float b0 = ffma(dy, fsub(a1, a0), a0);
     float b1 = ffma(dy, fsub(a3, a2), a2);
     return ffma(dx, fsub(b1, b0), b0);
+}
+
+// eval_gradient (fixed_interpolator.cpp:116-148) of the trilinear
+// interpolant in cell coordinates, normalised to -grad/|grad| (0 when the
+// gradient vanishes).  The reference takes finite differences 0.05 apart
+// (one-sided within 0.05 of a face); the interpolant is linear along each
+// axis, so every such difference is the exact partial derivative, which is
+// formed here directly from the corner differences.  The differences use
+// the values' float32 low parts when given (lo != nullptr): the data's
+// float32 rounding would otherwise dominate the differences of smooth
+// fields.  Where the field is exactly flat the reference normalises its
+// rounding noise into an arbitrary direction; here the gradient is 0.  A
+// NaN corner (log10 of a non-positive vertex value) makes the gradient NaN.
+YTGB_HD void light_gradient(const float *__restrict__ p, const float *__restrict__ lo, int sy, int sx, float dx,
+                            float dy, float dz, float g[3]) {
+    float c[8], e[8];
+    YTGB_UNROLL
+    for (int q = 0; q < 8; q++) {
+        const int o = ((q >> 2) & 1) * sx + ((q >> 1) & 1) * sy + (q & 1);
+        c[q] = ldg(p + o);
+        e[q] = lo ? ldg(lo + o) : 0.0f;
+    }
+    // corner q = 4a + 2b + c at offsets a (x), b (y), c (z)
+#define YTGB_D(u, v) fadd(fsub(c[u], c[v]), fsub(e[u], e[v]))
+    const float x00 = YTGB_D(4, 0), x01 = YTGB_D(5, 1), x10 = YTGB_D(6, 2), x11 = YTGB_D(7, 3);
+    const float y00 = YTGB_D(2, 0), y01 = YTGB_D(3, 1), y10 = YTGB_D(6, 4), y11 = YTGB_D(7, 5);
+    const float z00 = YTGB_D(1, 0), z01 = YTGB_D(3, 2), z10 = YTGB_D(5, 4), z11 = YTGB_D(7, 6);
+#undef YTGB_D
+    const float gx = ffma(dy, fsub(ffma(dz, fsub(x11, x10), x10), ffma(dz, fsub(x01, x00), x00)),
+                          ffma(dz, fsub(x01, x00), x00));
+    const float gy = ffma(dx, fsub(ffma(dz, fsub(y11, y10), y10), ffma(dz, fsub(y01, y00), y00)),
+                          ffma(dz, fsub(y01, y00), y00));
+    const float gz = ffma(dx, fsub(ffma(dy, fsub(z11, z10), z10), ffma(dy, fsub(z01, z00), z00)),
+                          ffma(dy, fsub(z01, z00), z00));
+    const float n2 = ffma(gz, gz, ffma(gy, gy, fmul(gx, gx)));
+    if (n2 > 0.0f && finitef(n2)) {
+        const float inv = fdiv(-1.0f, sqrtf(n2));
+        g[0] = fmul(gx, inv);
+        g[1] = fmul(gy, inv);
+        g[2] = fmul(gz, inv);
+    } else if (n2 == 0.0f) {
+        g[0] = g[1] = g[2] = 0.0f;
+    } else {
+        // a NaN (or infinite) corner: the reference's gradient is NaN, and so
+        // is every channel it composites (0 * NaN), as here
+        g[0] = g[1] = g[2] = __builtin_nanf("");
+    }
 }
 
 // FIT_get_value + FIT_eval_transfer's table combination
@@ -660,6 +726,42 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
     }
     float *xh = st.xh, *xl = st.xl;
     const bool comp = st.comp;
+    if (MODE == MODE_LIGHT) {
+        // LightSourceRenderSampler.sample (image_samplers.pyx:551-590): no
+        // mask test; all fields interpolated, the gradient of field 0
+        const int off = cur[0] * c.sx + cur[1] * c.sy + cur[2];
+        const int ns = a.n_samples;
+        const float dts = ns == 1 ? dtf : fdiv(dtf, (float)ns);
+        const float *lo = a.data_lo ? a.data_lo + (c.base - a.data) + off : nullptr;
+        for (int s = 0; s < ns; s++) {
+            const float f = fmul(dts, (float)s + 0.5f);
+            const float fx = fminf(fmaxf(ffma(f, c.vel[0], P[0]), 0.0f), 1.0f);
+            const float fy = fminf(fmaxf(ffma(f, c.vel[1], P[1]), 0.0f), 1.0f);
+            const float fz = fminf(fmaxf(ffma(f, c.vel[2], P[2]), 0.0f), 1.0f);
+            float dvs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            YTGB_UNROLL
+            for (int fi = 0; fi < 6; fi++)
+                if (fi < c.nf) dvs[fi] = trilinear(c.base + fi * c.fstride + off, c.sy, c.sx, fx, fy, fz);
+            float g[3];
+            light_gradient(c.base + off, lo, c.sy, c.sx, fx, fy, fz, g);
+            const float dot = ffma(a.light_dir[2], g[2], ffma(a.light_dir[1], g[1], fmul(a.light_dir[0], g[0])));
+            float trgba[6];
+            tf_eval(a.tf, s_tab, dvs, trgba);
+            if (a.tf.grey_opacity == 1) {
+                const float d = fmul(dts, fadd(fadd(trgba[0], trgba[1]), trgba[2]));
+                YTGB_UNROLL
+                for (int ch = 0; ch < 3; ch++)
+                    acc_light(xh[ch], xl[ch], d, fmul(trgba[ch], ffma(dot, a.light_rgba[ch], 1.0f)), comp);
+            } else {
+                YTGB_UNROLL
+                for (int ch = 0; ch < 3; ch++)
+                    acc_light(xh[ch], xl[ch], fmul(dts, trgba[ch]),
+                              fmul(trgba[ch], ffma(dot, a.light_rgba[ch], 1.0f)), comp);
+            }
+            st.touched |= 0x7u;
+        }
+        return;
+    }
     if (MODE == MODE_PROJ || MODE == MODE_MIP) {
         const int di = (cur[0] * c.dims[1] + cur[1]) * c.dims[2] + cur[2];
         const int nch = c.nf < 4 ? c.nf : 4;

@@ -88,7 +88,7 @@ __device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, i
     const ytgb_view &v = a.view;
     const int tid = threadIdx.x;
     if (tid < 4) sm.cnt[tid] = 0;
-    if (MODE == MODE_VR) {
+    if (MODE == MODE_VR || MODE == MODE_LIGHT) {
         // stage the transfer function unless this block already holds it
         const float *src = a.tf_tables;
         const bool reload = sm.tab_src != src || sm.tab_ctf != CTF;
@@ -254,7 +254,7 @@ int check_args(const ytgb_render_args *a, bool trace) {
         ytgb_set_error("ytgb_render: empty image");
         return YTGB_ERR_INVALID;
     }
-    if (a->kind < 0 || a->kind > 3) {
+    if (a->kind < 0 || a->kind > 4) {
         ytgb_set_error("ytgb_render: unknown sampler kind");
         return YTGB_ERR_INVALID;
     }
@@ -283,7 +283,8 @@ int check_args(const ytgb_render_args *a, bool trace) {
     if (misaligned(a->rects, 16) || misaligned(a->tf_tables, 16) || misaligned(a->bricks, 16) ||
         misaligned(a->bounds, 8) || misaligned(a->image, 8) || misaligned(a->zbuffer, 8) ||
         misaligned(a->counters, 8) || misaligned(v.px_pos, 8) || misaligned(v.px_dir, 8) ||
-        misaligned(a->order, 4) || misaligned(a->data, 4) || misaligned(a->error, 4)) {
+        misaligned(a->order, 4) || misaligned(a->data, 4) || misaligned(a->error, 4) ||
+        misaligned(a->data_lo, 4)) {
         ytgb_set_error("ytgb_render: misaligned pointer (rects, tf_tables and bricks need 16 bytes, "
                        "float64 arrays 8)");
         return YTGB_ERR_INVALID;
@@ -292,15 +293,16 @@ int check_args(const ytgb_render_args *a, bool trace) {
         ytgb_set_error("ytgb_render: missing cell-boundary tables");
         return YTGB_ERR_INVALID;
     }
-    if (!trace && a->kind == YTGB_VOLUME_RENDER && !a->tf_tables) {
+    if (!trace && (a->kind == YTGB_VOLUME_RENDER || a->kind == YTGB_LIGHT_SOURCE) && !a->tf_tables) {
         ytgb_set_error("ytgb_render: volume rendering needs a transfer function");
         return YTGB_ERR_INVALID;
     }
     return YTGB_OK;
 }
 
-// Transfer-function header checks and the shared-memory bytes its tables take.
-int tf_check(const ytgb_tf &t, size_t *smem) {
+// Transfer-function header checks and the shared-memory bytes its tables take
+// (in the packed ColorTransferFunction layout when ctf_layout).
+int tf_check(const ytgb_tf &t, size_t *smem, bool ctf_layout) {
     if (t.n_fits < 0 || t.n_fits > 6 || t.nbins_max < 2 || t.nbins_max > YTGB_TF_MAX_BINS) {
         ytgb_set_error("inconsistent transfer function header");
         return YTGB_ERR_INVALID;
@@ -323,7 +325,7 @@ int tf_check(const ytgb_tf &t, size_t *smem) {
         ytgb_set_error("ctf_fast set on tables that are not a ColorTransferFunction");
         return YTGB_ERR_INVALID;
     }
-    *smem = t.ctf_fast ? (size_t)3 * t.nbins_max * sizeof(float4) : (size_t)t.n_fits * t.nbins_max * sizeof(float4);
+    *smem = ctf_layout ? (size_t)3 * t.nbins_max * sizeof(float4) : (size_t)t.n_fits * t.nbins_max * sizeof(float4);
     if (*smem > 200 * 1024) {
         ytgb_set_error("transfer-function tables exceed 200 KB of shared memory");
         return YTGB_ERR_INVALID;
@@ -413,9 +415,14 @@ extern "C" int ytgb_render(const ytgb_render_args *a, void *stream) {
         ytgb_set_error("ytgb_render: unknown tile shape");
         return YTGB_ERR_INVALID;
     }
+    if (a->kind == YTGB_LIGHT_SOURCE) {
+        size_t smem = 0;
+        if ((st = tf_check(a->tf, &smem, false))) return st;
+        return launch_ts<MODE_LIGHT, 0>(ts, a, smem, s, nullptr, nullptr);
+    }
     if (a->kind == YTGB_VOLUME_RENDER) {
         size_t smem = 0;
-        if ((st = tf_check(a->tf, &smem))) return st;
+        if ((st = tf_check(a->tf, &smem, a->tf.ctf_fast != 0))) return st;
         return a->tf.ctf_fast ? launch_ts<MODE_VR, 1>(ts, a, smem, s, nullptr, nullptr)
                               : launch_ts<MODE_VR, 0>(ts, a, smem, s, nullptr, nullptr);
     }
@@ -455,9 +462,9 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
             ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler and table layout");
             return YTGB_ERR_INVALID;
         }
-        if (kind == YTGB_VOLUME_RENDER) {
+        if (kind == YTGB_VOLUME_RENDER || kind == YTGB_LIGHT_SOURCE) {
             size_t sm = 0;
-            if (int st = tf_check(a.tf, &sm)) return st;
+            if (int st = tf_check(a.tf, &sm, kind == YTGB_VOLUME_RENDER && ctf != 0)) return st;
             smem = sm > smem ? sm : smem;
         }
         const int tx = (a.view.nx + TX - 1) / TX, ty = (a.view.ny + TY - 1) / TY;
@@ -479,7 +486,7 @@ extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, i
                                  int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                                  int32_t blocks, void *stream) {
     if (!d_entries || n <= 0 || total_tiles <= 0 || !d_queue || tile_shape < 0 || tile_shape > 2 || kind < 0 ||
-        kind > 3 || smem_bytes < 0 || smem_bytes > 200 * 1024 || ((uintptr_t)d_entries & 15) != 0 ||
+        kind > 4 || smem_bytes < 0 || smem_bytes > 200 * 1024 || ((uintptr_t)d_entries & 15) != 0 ||
         ((uintptr_t)d_queue & 3) != 0) {
         ytgb_set_error("ytgb_batch_render: bad arguments");
         return YTGB_ERR_INVALID;
@@ -495,6 +502,8 @@ extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, i
     case YTGB_VOLUME_RENDER:
         return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s)
                         : batch_launch_ts<MODE_VR, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s);
+    case YTGB_LIGHT_SOURCE:
+        return batch_launch_ts<MODE_LIGHT, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s);
     case YTGB_PROJECTION:
         return batch_launch_ts<MODE_PROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
     case YTGB_INTERPOLATED_PROJECTION:
@@ -573,7 +582,7 @@ extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int3
                        " views); split the batch or use ytgb_batch_render with a caller-allocated table");
         return YTGB_ERR_INVALID;
     }
-    if (!h_entries || n <= 0 || total_tiles <= 0 || tile_shape < 0 || tile_shape > 2 || kind < 0 || kind > 3 ||
+    if (!h_entries || n <= 0 || total_tiles <= 0 || tile_shape < 0 || tile_shape > 2 || kind < 0 || kind > 4 ||
         smem_bytes < 0 || smem_bytes > 200 * 1024) {
         ytgb_set_error("ytgb_batch_render_noalloc: bad arguments");
         return YTGB_ERR_INVALID;
@@ -597,6 +606,8 @@ extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int3
     case YTGB_VOLUME_RENDER:
         return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s)
                         : batch_launch_ts<MODE_VR, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
+    case YTGB_LIGHT_SOURCE:
+        return batch_launch_ts<MODE_LIGHT, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
     case YTGB_PROJECTION:
         return batch_launch_ts<MODE_PROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
     case YTGB_INTERPOLATED_PROJECTION:

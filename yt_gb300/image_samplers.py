@@ -112,6 +112,7 @@ def brick_tuple(pg):
 
 class ImageSampler:
     kind = None
+    _with_lo = False
 
     def __init__(self, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, *args,
                  **kwargs):
@@ -181,6 +182,9 @@ class ImageSampler:
     def _tf(self):
         return None
 
+    def _light(self):
+        return None
+
     def flush(self):
         if not self._pending:
             return
@@ -188,7 +192,7 @@ class ImageSampler:
         dev = _device()
         L = _lib.lib()
         t0 = time.perf_counter()
-        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev)
+        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev, with_lo=self._with_lo)
         order = np.arange(len(pending), dtype=np.int32)
         nx, ny = self.nv
         t1 = time.perf_counter()
@@ -228,7 +232,7 @@ class ImageSampler:
         t2 = time.perf_counter()
         _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb_d,
                 n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
-                px_pos=px_pos, px_dir=px_dir)
+                px_pos=px_pos, px_dir=px_dir, light=self._light())
         stream = torch.cuda.current_stream(dev)
         _lib.check(L.ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
         t3 = time.perf_counter()
@@ -299,3 +303,32 @@ class VolumeRenderSampler(ImageSampler):
 
     def _tf(self):
         return self._packed
+
+
+class LightSourceRenderSampler(ImageSampler):
+    """Volume rendering with a directional light on the gradient of field 0
+    (image_samplers.pyx:496-590; eval_gradient, fixed_interpolator.cpp:
+    116-148; FIT_eval_transfer_with_light, field_interpolation_tables.pxd:
+    115-143).  ``light_dir`` is normalised as yt does.  ``gradient_lo``
+    also uploads each value's float32 rounding error so the gradient's
+    differences carry float64 accuracy (for fields whose cell-to-cell
+    variation is near float32's resolution)."""
+    kind = _lib.LIGHT_SOURCE
+
+    def __init__(self, vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, tf_obj,
+                 n_samples=10, light_dir=(1.0, 1.0, 1.0), light_rgba=(1.0, 1.0, 1.0, 1.0), gradient_lo=False,
+                 **kwargs):
+        super().__init__(vp_pos, vp_dir, center, bounds, image, x_vec, y_vec, width, volume_method, **kwargs)
+        assert tf_obj.n_field_tables <= 6
+        self.tf_obj = tf_obj
+        self.n_samples = int(n_samples)
+        self._packed = _tfm.pack(tf_obj)
+        self.light_dir = np.asarray(light_dir, dtype=np.float64)
+        self.light_rgba = np.asarray(light_rgba, dtype=np.float64)
+        self._with_lo = bool(gradient_lo)
+
+    def _tf(self):
+        return self._packed
+
+    def _light(self):
+        return (self.light_dir, self.light_rgba)

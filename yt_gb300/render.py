@@ -46,7 +46,7 @@ class Renderer:
         return self.kdtree.viewpoint_order(camera.viewpoint)
 
     def render(self, camera, kind=_lib.VOLUME_RENDER, n_samples=1, order=None, image=None, zbuffer=None,
-               flags=0, stream=None, keep=None, device_rays=True, tile_shape=None):
+               flags=0, stream=None, keep=None, device_rays=True, tile_shape=None, light=None):
         """Render one view.  ``tile_shape`` None takes the tuned shape of the
         view's workload class (``yt_gb300/tuning.json``) unless ``flags``
         already carries one."""
@@ -67,11 +67,13 @@ class Renderer:
             px_dir = torch.from_numpy(pdir).to(self.device, non_blocking=False)
             if keep is not None:
                 keep += [px_pos, px_dir]
-        tf = self.packed if kind == _lib.VOLUME_RENDER else None
-        if kind == _lib.VOLUME_RENDER and tf is None:
+        uses_tf = kind in (_lib.VOLUME_RENDER, _lib.LIGHT_SOURCE)
+        tf = self.packed if uses_tf else None
+        if uses_tf and tf is None:
             raise ValueError("volume rendering needs a transfer function")
         _render(self.bricks, view, order, kind, image, tf=tf, zbuffer=zbuffer, n_samples=n_samples, flags=flags,
-                counters=self.counters, error=self.error, px_pos=px_pos, px_dir=px_dir, stream=stream, keep=keep)
+                counters=self.counters, error=self.error, px_pos=px_pos, px_dir=px_dir, stream=stream, keep=keep,
+                light=light)
         return image
 
     def check(self):
@@ -92,11 +94,19 @@ class Renderer:
 def relative_error(gpu: np.ndarray, ref: np.ndarray, tau: float = 1e-6, channels=(0, 1, 2, 3)):
     """Per-pixel relative error max|g-o| / max(|o|, tau*max|o|) and its RMS over
     pixels with o != 0, per channel; returns (max over channels, rms over
-    channels)."""
+    channels).  NaN pixels must coincide (a NaN against a number is an
+    infinite error) and are otherwise left out."""
     mx, rms = 0.0, 0.0
     for c in channels:
         o = ref[..., c]
         g = gpu[..., c]
+        on, gn = np.isnan(o), np.isnan(g)
+        if not np.array_equal(on, gn):
+            return float("inf"), float("inf")
+        keep = ~on
+        o, g = o[keep], g[keep]
+        if o.size == 0:
+            continue
         m = np.abs(o).max()
         if m == 0:
             e = np.abs(g).max()

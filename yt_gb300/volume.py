@@ -55,7 +55,7 @@ class BrickSet:
     samplers index them exactly as yt does), ``mask`` a uint8 array of
     ``dims`` or None (all ones)."""
 
-    def __init__(self, bricks: Sequence, device="cuda"):
+    def __init__(self, bricks: Sequence, device="cuda", with_lo=False):
         self.device = torch.device(device)
         n = len(bricks)
         self.n = n
@@ -116,13 +116,18 @@ class BrickSet:
         sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
         desc, stride, data_off, total, bounds = self._layout(dims, le, re, nfields, sizes_min, sizes_max)
         buf = _pinned((max(total, 4),), torch.float32, self.device)
+        buf_lo = _pinned((max(total, 4),), torch.float32, self.device) if with_lo else None
         L = _lib.lib()
         # float64 -> float32 gather into the pinned arena, on all host cores
         src = np.array(fptr, dtype=np.uintp)
         fbrick = np.repeat(np.arange(n), nfields[:n])
         dst_f = (data_off[fbrick] + (np.arange(len(fptr)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
-        _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
-                                      buf.data_ptr(), 0), "ytgb_pack_fields")
+        if with_lo:
+            _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
+                                                buf.data_ptr(), buf_lo.data_ptr(), 0), "ytgb_pack_fields_split")
+        else:
+            _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
+                                          buf.data_ptr(), 0), "ytgb_pack_fields")
         # masks: kept only when some cell is masked out
         mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
         desc["mask_offset"][:] = -1
@@ -142,15 +147,16 @@ class BrickSet:
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
         self.data = buf.to(self.device, non_blocking=True)
+        self.data_lo = buf_lo.to(self.device, non_blocking=True) if buf_lo is not None else None
         self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
         self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
         self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
         self.nbytes = int(self.data.numel() * 4)
-        self.upload_bytes = int(self.data.numel() * 4 + self.bounds.numel() * 8 + self.desc.numel() +
-                                (self.masks.numel() if self.masks is not None else 0))
+        self.upload_bytes = int(self.data.numel() * 4 * (2 if with_lo else 1) + self.bounds.numel() * 8 +
+                                self.desc.numel() + (self.masks.numel() if self.masks is not None else 0))
 
     @classmethod
-    def on_device(cls, dims, le, re, device="cuda", n_fields=1):
+    def on_device(cls, dims, le, re, device="cuda", n_fields=1, with_lo=False):
         """Bricks of the given geometry whose vertex-centred fields are
         written on the device (``AMRKDTree.device_brickset``): descriptors and
         boundary tables as usual, a float32 arena of (dims+1)^3 values per
@@ -177,6 +183,7 @@ class BrickSet:
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
         self.data = torch.empty(max(total, 4), dtype=torch.float32, device=self.device)
+        self.data_lo = torch.empty_like(self.data) if with_lo else None
         self.masks = None
         self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
         self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
@@ -236,6 +243,25 @@ class BrickSet:
         return out
 
 
+def normalised_light(light_dir) -> np.ndarray:
+    """LightSourceRenderSampler.__cinit__'s normalisation (image_samplers.pyx:
+    530-532), in float64."""
+    ld = np.asarray(light_dir, dtype=np.float64)
+    return ld / np.sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2])
+
+
+def set_light(args, bricks, light):
+    """Fill the light-source fields of a ytgb_render_args: ``light`` is
+    (light_dir, light_rgba) or None for yt's defaults ((1,1,1), (1,1,1,1))."""
+    ld, rgba = light if light is not None else ((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0))
+    ld = normalised_light(ld)
+    for i in range(3):
+        args.light_dir[i] = float(ld[i])
+    for i in range(4):
+        args.light_rgba[i] = float(rgba[i])
+    args.data_lo = _ptr(bricks.data_lo)
+
+
 def _ptr(t):
     return None if t is None else t.data_ptr()
 
@@ -248,7 +274,8 @@ def check_inputs(bricks: BrickSet, view: _lib.View, order, kind, image=None, zbu
     if order.size and (order.min() < 0 or order.max() >= bricks.n):
         raise ValueError("order entry out of range")
     used = np.unique(order) if order.size else order
-    need = bricks.verts if kind in (_lib.VOLUME_RENDER, _lib.INTERPOLATED_PROJECTION) else bricks.cells
+    need = (bricks.verts if kind in (_lib.VOLUME_RENDER, _lib.INTERPOLATED_PROJECTION, _lib.LIGHT_SOURCE)
+            else bricks.cells)
     short = used[bricks.min_elems[used] < need[used]] if used.size else used
     if short.size:
         k = int(short[0])
@@ -271,7 +298,7 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
            counters: torch.Tensor | None = None, error: torch.Tensor | None = None,
            px_pos: torch.Tensor | None = None, px_dir: torch.Tensor | None = None,
            stream: torch.cuda.Stream | None = None, rects: np.ndarray | None = None,
-           keep: list | None = None) -> None:
+           keep: list | None = None, light=None) -> None:
     """Launch ytgb_render for one view.  ``image`` is a (nx, ny, 4) float64
     device tensor updated in place; ``tf`` a PackedTF for volume rendering.
     Device temporaries that must outlive the asynchronous launch are appended
@@ -308,6 +335,8 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
         args.tf_tables = tf.device_tables(dev).data_ptr()
     args.image = image.data_ptr()
     args.zbuffer = _ptr(zbuffer)
+    if kind == _lib.LIGHT_SOURCE:
+        set_light(args, bricks, light)
     args.counters = _ptr(counters)
     args.error = _ptr(error)
     st = _lib.lib().ytgb_render(C.byref(args), C.c_void_p(stream.cuda_stream))
