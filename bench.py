@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--cpu-res", type=int, default=0, help="resolution of the CPU-baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="amr_vr", choices=["amr_vr", "multiview", "projection", "serve", "prep"],
+    ap.add_argument("--workload", default="amr_vr", choices=["amr_vr", "multiview", "projection", "serve", "prep", "octree"],
                     help="amr_vr (default, the headline frame); the others print their own line")
     ap.add_argument("--tile-shape", type=int, default=-1, help="-1: from the autotuning table")
     ap.add_argument("--n-requests", type=int, default=400)
@@ -737,6 +737,122 @@ def run_prep(args):
     print(json.dumps(line), flush=True)
 
 
+def run_octree(args):
+    """The octree path (cast_through_octree): a 217k-cell octree dataset
+    (levels 5-9, cells refined where the blob field exceeds the 85th
+    percentile of their level), perspective 1024^2, VolumeRenderSampler with
+    an 8-layer ColorTransferFunction; device time per frame, yt's compiled
+    octree sampler (on a 128^2 sample of the same camera, all host threads)
+    and the oracle's float64 image of that sample for the error."""
+    import torch
+
+    from oracle import cpu as ocpu
+    from yt_gb300 import _lib, testing, workloads
+    from yt_gb300.camera import Camera
+    from yt_gb300.octree import Octree, OctreeVolume, render_octree
+    from yt_gb300.render import relative_error
+    from yt_gb300.transfer_functions import pack
+
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    depth, ipos, lvl, cells = testing.octree_cells(base_level=5, max_level=9, seed=0, percentile=85.0)
+    oc = Octree(np.zeros(3), np.ones(3), depth)
+    oc.add_nodes(ipos, lvl, np.arange(ipos.shape[0], dtype=np.int32))
+    vol = OctreeVolume(oc, cells, dev)
+    vmin, vmax = float(cells[:, :8].min()), float(cells[:, :8].max())
+    tf = workloads.color_tf((vmin, vmax), 8)
+    packed = pack(tf)
+    t_build = time.time() - t0
+    res = args.res
+    cam = Camera((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), res, lens_type="perspective")
+    view = cam.device_view()
+    img = torch.zeros((res, res, 4), dtype=torch.float64, device=dev)
+    counters = torch.zeros(4, dtype=torch.int64, device=dev)
+    error = torch.zeros(1, dtype=torch.int32, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        img.zero_()
+        render_octree(vol, view, _lib.VOLUME_RENDER, img, tf=packed, counters=counters, error=error)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    counters.zero_()
+    steps = max(1, min(args.steps, 20))
+    evs = []
+    clocks = ClockSampler(0)
+    with clocks:
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    assert int(error.item()) == 0
+    ms = np.array([a.elapsed_time(b) for a, b in evs])
+    samples = int(counters[0].item()) // steps
+    # CPU: yt's compiled octree sampler on a bounded sample of the view
+    cres = max(32, res // 8)
+    ccam = Camera(cam.position, cam.focus, cam.width, cres, lens_type="perspective")
+    p = ccam.sampler_params()
+    cpu = {"value": None, "kind": None}
+    threads = os.cpu_count() or 1
+    try:
+        ref_pkg = ROOT / "oracle" / "_ref" / "pkg"
+        if not any((ref_pkg / "yt" / "utilities" / "lib").glob("image_samplers*.so")):
+            raise ImportError("reference sampler not built")
+        sys.path.insert(0, str(ref_pkg))
+        from yt.utilities.lib import image_samplers as RIS  # noqa: PLC0415
+        from yt.utilities.lib._octree_raytracing import _OctreeRayTracing  # noqa: PLC0415
+        from yt.utilities.lib.partitioned_grid import PartitionedGrid  # noqa: PLC0415
+
+        roc = _OctreeRayTracing(np.zeros(3), np.ones(3), depth)
+        roc.add_nodes(ipos, lvl, np.arange(ipos.shape[0], dtype=np.int32))
+        dt = cells.reshape(1, -1, 14, 1)
+        pg = PartitionedGrid(0, dt, np.ones(dt.shape[1:], dtype=np.uint8), np.zeros(3), np.ones(3),
+                             np.array([1, 1, 1], dtype="int64"), n_fields=1)
+        rimg = np.zeros((cres, cres, 4))
+        s = RIS.VolumeRenderSampler(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], rimg, p["x_vec"],
+                                    p["y_vec"], p["width"], "Octree", tf, 1, lens_type=p["lens_type"],
+                                    camera_data=p["camera_data"], zbuffer=np.ones((cres, cres)))
+        tc = time.perf_counter()
+        s(pg, oct=roc, num_threads=threads)
+        dtc = time.perf_counter() - tc
+        cpu["kind"] = "reference"
+    except ImportError:
+        dtc = None
+    so = ocpu.OracleSampler("volume_render", p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"],
+                            p["x_vec"], p["y_vec"], p["width"], lens_type=p["lens_type"],
+                            camera_data=p["camera_data"], tf=tf)
+    tc = time.perf_counter()
+    cvis = ocpu.render_octree(so, cells, ocpu.OracleOctree(depth, np.zeros(3), np.ones(3), ipos, lvl))
+    dto = time.perf_counter() - tc
+    if dtc is None:
+        dtc, cpu["kind"] = dto, "port"
+    cpu["value"] = cvis / dtc / 1e9
+    # GPU image of the same sample against the oracle
+    gimg = torch.zeros((cres, cres, 4), dtype=torch.float64, device=dev)
+    render_octree(vol, ccam.device_view(), _lib.VOLUME_RENDER, gimg, tf=packed)
+    mx, rms = relative_error(gimg.cpu().numpy(), p["image"], channels=(0, 1, 2))
+    line = {"metric": "Gsamples/s", "workload": "octree", "value": samples / (ms.mean() / 1e3) / 1e9,
+            "unit": "Gsamples/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": float(ms.mean()), "higher_is_better": True, "samples_per_step": samples,
+            "cpu_baseline": {**cpu, "unit": "Gsamples/s", "cores": threads,
+                             "sample": f"the same camera at {cres}x{cres} ({cvis} samples)"},
+            "accuracy": {"max_rel_err": mx, "rms_rel_err": rms, "vs": f"float64 oracle at {cres}x{cres}"},
+            "clocks": clocks.summary(),
+            "config": {"workload": "octree: 217k cells, levels 5-9, perspective, 8-layer CTF, 1 sample/cell",
+                       "cells": int(cells.shape[0]), "nodes": int(vol.n_nodes), "depth": depth,
+                       "resolution": res, "l2": "flushed between steps (256 MiB write)"},
+            "build_seconds": t_build}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -749,5 +865,7 @@ if __name__ == "__main__":
         run_serve(a)
     elif a.workload == "prep":
         run_prep(a)
+    elif a.workload == "octree":
+        run_octree(a)
     else:
         run_ours(a)

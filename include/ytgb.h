@@ -284,6 +284,55 @@ int ytgb_host_copy(void *dst, const void *src, int64_t bytes, int32_t n_threads)
  * made writing a 32 MiB image ~12 ms instead of ~0.7 ms. */
 int ytgb_host_prefault(void *p, int64_t bytes);
 
+/* ---- octree volumes --------------------------------------------------------- */
+/* One node of an octree as built by ytgb_octree_build: children (-1 none,
+ * index iflat = 4x + 2y + z of the child octant), the cell key of a terminal
+ * node, flags (bit 0 terminal, bit 1 has children). */
+typedef struct ytgb_onode {
+    int32_t child[8];
+    int32_t key;
+    int32_t flags;
+} ytgb_onode;
+
+/* An octree volume on the device: the nodes, and per cell (key) its 8
+ * vertex values (float32, (i,j,k) C order) and 9 float64 edge values (left
+ * edge, right edge, 1/(right - left)) -- the 14 values per cell of yt's
+ * octree volume source (render_source.py:667-680) split by precision. */
+typedef struct ytgb_octree_args {
+    const ytgb_onode *nodes;
+    const float *verts;
+    const double *edges;
+    int32_t n_nodes;
+    int32_t n_cells;
+    int32_t depth;
+    int32_t pad;
+    double dle[3];
+    double dre[3];
+} ytgb_octree_args;
+
+/* Replaces _OctreeRayTracing(LE, RE, depth).add_nodes(ipos, lvl, key)
+ * (_octree_raytracing.pyx:14-31; Octree::insert_node and create_get_node,
+ * _octree_raytracing.hpp:139-175, 238-257): nodes are numbered in creation
+ * order, the root first.  Returns a handle (NULL on bad input). */
+void *ytgb_octree_build(int32_t depth, const double *dle, const double *dre, const int32_t *ipos,
+                        const int32_t *lvl, const int32_t *key, int64_t n);
+int64_t ytgb_octree_num_nodes(void *tree);
+int ytgb_octree_nodes(void *tree, ytgb_onode *out);
+void ytgb_octree_destroy(void *tree);
+
+/* Replaces ImageSampler.cast_through_octree (image_samplers.pyx:202-288):
+ * every pixel's ray cast through the octree (Octree::cast_ray,
+ * _octree_raytracing.hpp:199-230, 276-366) and each terminal cell handed to
+ * the sampler of args->kind as a 1x1x1 brick, in traversal order.  The rays
+ * are per-pixel (YTGB_LENS_PER_PIXEL or YTGB_LENS_PERSPECTIVE; the
+ * reference reads per-pixel ray arrays).  args->data must be o->verts;
+ * bricks, order and rects are unused. */
+int ytgb_render_octree(const ytgb_render_args *args, const ytgb_octree_args *o, void *stream);
+/* Traversal trace of the octree path: per pixel an FNV-1a hash over (cell
+ * key, enter t bits, exit t bits) of every cell sampled, and the count. */
+int ytgb_trace_octree(const ytgb_render_args *args, const ytgb_octree_args *o, unsigned long long *hashes,
+                      long long *counts, void *stream);
+
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
  * amr_kdtools.Node.add_grids / insert_grids / split_grids /

@@ -288,3 +288,53 @@ def trace_rays(brick, pos, dirs, max_t, cap):
     lib().yo_trace_rays(C.byref(ob.vcs[0]), _ptr(pos), _ptr(dirs), _ptr(max_t), n, cap,
                         _ptr(counts, C.c_int64), _ptr(cells, C.c_int32), _ptr(ts))
     return counts, cells, ts
+
+
+class OracleOctree:
+    """Octree<int> of _octree_raytracing.hpp (yo_octree_build): cells
+    inserted at (ipos, lvl) with their keys."""
+
+    def __init__(self, depth, le, re, ipos, lvl, key=None):
+        L = lib()
+        L.yo_octree_build.restype = C.c_void_p
+        L.yo_octree_build.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_int64]
+        L.yo_octree_free.argtypes = [C.c_void_p]
+        ipos = np.ascontiguousarray(ipos, dtype=np.int32).reshape(-1, 3)
+        lvl = np.ascontiguousarray(lvl, dtype=np.int32)
+        key = np.arange(ipos.shape[0], dtype=np.int32) if key is None else np.ascontiguousarray(key, dtype=np.int32)
+        le = np.ascontiguousarray(le, dtype=np.float64)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        self.h = L.yo_octree_build(int(depth), le.ctypes.data, re.ctypes.data, ipos.ctypes.data, lvl.ctypes.data,
+                                   key.ctypes.data, ipos.shape[0])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().yo_octree_free(self.h)
+            self.h = None
+
+
+def render_octree(sampler: "OracleSampler", cells: np.ndarray, octree: OracleOctree, num_threads=0) -> int:
+    """ImageSampler.cast_through_octree (image_samplers.pyx:202-288) into the
+    sampler's image; returns the number of cells sampled."""
+    L = lib()
+    L.yo_cast_through_octree.restype = C.c_int64
+    L.yo_cast_through_octree.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    cells = np.ascontiguousarray(cells, dtype=np.float64)
+    return int(L.yo_cast_through_octree(C.byref(sampler.s), cells.ctypes.data, octree.h, int(num_threads), None,
+                                        None))
+
+
+def trace_octree(sampler: "OracleSampler", cells: np.ndarray, octree: OracleOctree, num_threads=0):
+    """Per pixel: FNV-1a hash over (cell key, enter bits, exit bits) of the
+    cells cast_through_octree samples, and their count."""
+    L = lib()
+    L.yo_cast_through_octree.restype = C.c_int64
+    L.yo_cast_through_octree.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    nx, ny = sampler.s.nv[0], sampler.s.nv[1]
+    hashes = np.full(nx * ny, 1469598103934665603, dtype=np.uint64)
+    counts = np.zeros(nx * ny, dtype=np.int64)
+    cells = np.ascontiguousarray(cells, dtype=np.float64)
+    L.yo_cast_through_octree(C.byref(sampler.s), cells.ctypes.data, octree.h, int(num_threads),
+                             hashes.ctypes.data, counts.ctypes.data)
+    return hashes.reshape(nx, ny), counts.reshape(nx, ny)

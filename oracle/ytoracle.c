@@ -807,3 +807,287 @@ void yo_trace_rays(const yo_vc *vc, const double *pos, const double *dir, const 
         counts[i] = r.n;
     }
 }
+
+/* ---- octree ray casting --------------------------------------------------
+ * Octree<int> of _octree_raytracing.hpp (insert_node :139-175,
+ * create_get_node :238-257, cast_ray :199-230, proc_subtree :276-337,
+ * first_node / next_node :340-366) and ImageSampler.cast_through_octree
+ * (image_samplers.pyx:202-288).  Nodes live in one array; children are
+ * indices (-1: none) allocated lazily as the reference allocates them. */
+typedef struct {
+    int32_t child[8];
+    int32_t has_children;
+    int32_t terminal;
+    int32_t key;
+} yo_onode;
+
+typedef struct {
+    yo_onode *nodes;
+    int64_t n, cap;
+    int depth;
+    double dle[3], dre[3], size[3];
+} yo_octree;
+
+static int32_t yo_onode_new(yo_octree *t)
+{
+    if (t->n == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 64;
+        t->nodes = (yo_onode *)realloc(t->nodes, (size_t)t->cap * sizeof(yo_onode));
+    }
+    yo_onode *nd = &t->nodes[t->n];
+    for (int i = 0; i < 8; i++) nd->child[i] = -1;
+    nd->has_children = 0;
+    nd->terminal = 0;
+    nd->key = 0;
+    return (int32_t)t->n++;
+}
+
+void *yo_octree_build(int depth, const double *dle, const double *dre, const int32_t *ipos, const int32_t *lvl,
+                      const int32_t *key, int64_t n)
+{
+    yo_octree *t = (yo_octree *)calloc(1, sizeof(yo_octree));
+    int64_t c;
+    t->depth = depth;
+    for (int i = 0; i < 3; i++) {
+        t->dle[i] = dle[i];
+        t->dre[i] = dre[i];
+        t->size[i] = dre[i] - dle[i];
+    }
+    yo_onode_new(t); /* the root */
+    for (c = 0; c < n; c++) {
+        uint64_t mask = 1u << (depth - 1);
+        int32_t node = 0;
+        for (int ibit = depth - 1; ibit >= depth - lvl[c]; --ibit) {
+            int iflat = 0;
+            for (int d = 0; d < 3; d++) {
+                iflat += (ipos[3 * c + d] & mask) != 0;
+                iflat <<= 1;
+            }
+            iflat >>= 1;
+            mask >>= 1;
+            t->nodes[node].has_children = 1;
+            if (t->nodes[node].child[iflat] < 0) {
+                int32_t nn = yo_onode_new(t);
+                t->nodes[node].child[iflat] = nn;
+            }
+            node = t->nodes[node].child[iflat];
+        }
+        t->nodes[node].terminal = 1;
+        t->nodes[node].key = key[c];
+    }
+    return t;
+}
+
+void yo_octree_free(void *h)
+{
+    yo_octree *t = (yo_octree *)h;
+    if (!t) return;
+    free(t->nodes);
+    free(t);
+}
+
+static inline double yo_smax(double a, double b) { return (a < b) ? b : a; } /* std::max */
+static inline double yo_smin(double a, double b) { return (b < a) ? b : a; } /* std::min */
+
+static int yo_first_node(double tx0, double ty0, double tz0, double txm, double tym, double tzm)
+{
+    int index = 0;
+    if (tx0 >= yo_smax(ty0, tz0)) {
+        if (tym < tx0) index |= 2;
+        if (tzm < tx0) index |= 1;
+    } else if (ty0 >= yo_smax(tx0, tz0)) {
+        if (txm < ty0) index |= 4;
+        if (tzm < ty0) index |= 1;
+    } else {
+        if (txm < tz0) index |= 4;
+        if (tym < tz0) index |= 2;
+    }
+    return index;
+}
+
+static int yo_next_node(double tx, double ty, double tz, int ix, int iy, int iz)
+{
+    if (tx < yo_smin(ty, tz)) return ix;
+    if (ty < yo_smin(tx, tz)) return iy;
+    return iz;
+}
+
+typedef void (*yo_ocell_fn)(void *ctx, int32_t key, double t_in, double t_out);
+
+static void yo_proc_subtree(const yo_octree *t, double tx0, double ty0, double tz0, double tx1, double ty1,
+                            double tz1, int32_t n, int a, yo_ocell_fn fn, void *ctx)
+{
+    double txm, tym, tzm;
+    int iNode;
+    if (tx1 < 0 || ty1 < 0 || tz1 < 0) return;
+    if (n < 0) return;
+    const yo_onode *nd = &t->nodes[n];
+    if (nd->terminal) {
+        fn(ctx, nd->key, yo_smax(yo_smax(tx0, ty0), tz0), yo_smin(yo_smin(tx1, ty1), tz1));
+        return;
+    }
+    if (!nd->has_children) return;
+    txm = (tx0 + tx1) * 0.5;
+    tym = (ty0 + ty1) * 0.5;
+    tzm = (tz0 + tz1) * 0.5;
+    iNode = yo_first_node(tx0, ty0, tz0, txm, tym, tzm);
+    do {
+        switch (iNode) {
+        case 0:
+            yo_proc_subtree(t, tx0, ty0, tz0, txm, tym, tzm, nd->child[a], a, fn, ctx);
+            iNode = yo_next_node(txm, tym, tzm, 4, 2, 1);
+            break;
+        case 1:
+            yo_proc_subtree(t, tx0, ty0, tzm, txm, tym, tz1, nd->child[1 ^ a], a, fn, ctx);
+            iNode = yo_next_node(txm, tym, tz1, 5, 3, 8);
+            break;
+        case 2:
+            yo_proc_subtree(t, tx0, tym, tz0, txm, ty1, tzm, nd->child[2 ^ a], a, fn, ctx);
+            iNode = yo_next_node(txm, ty1, tzm, 6, 8, 3);
+            break;
+        case 3:
+            yo_proc_subtree(t, tx0, tym, tzm, txm, ty1, tz1, nd->child[3 ^ a], a, fn, ctx);
+            iNode = yo_next_node(txm, ty1, tz1, 7, 8, 8);
+            break;
+        case 4:
+            yo_proc_subtree(t, txm, ty0, tz0, tx1, tym, tzm, nd->child[4 ^ a], a, fn, ctx);
+            iNode = yo_next_node(tx1, tym, tzm, 8, 6, 5);
+            break;
+        case 5:
+            yo_proc_subtree(t, txm, ty0, tzm, tx1, tym, tz1, nd->child[5 ^ a], a, fn, ctx);
+            iNode = yo_next_node(tx1, tym, tz1, 8, 7, 8);
+            break;
+        case 6:
+            yo_proc_subtree(t, txm, tym, tz0, tx1, ty1, tzm, nd->child[6 ^ a], a, fn, ctx);
+            iNode = yo_next_node(tx1, ty1, tzm, 8, 8, 7);
+            break;
+        case 7:
+            yo_proc_subtree(t, txm, tym, tzm, tx1, ty1, tz1, nd->child[7 ^ a], a, fn, ctx);
+            iNode = 8;
+            break;
+        }
+    } while (iNode < 8);
+}
+
+/* Octree::cast_ray (Ray normalises the direction, :49-64) */
+static void yo_octree_cast_ray(const yo_octree *t, const double *o_in, const double *d_in, yo_ocell_fn fn,
+                               void *ctx)
+{
+    double o[3], d[3], dd = 0, t0[3], t1[3], tmax0, tmin1;
+    int a = 0, bmask = 4, i;
+    for (i = 0; i < 3; i++) o[i] = o_in[i];
+    for (i = 0; i < 3; i++) dd += d_in[i] * d_in[i];
+    dd = sqrt(dd);
+    for (i = 0; i < 3; i++) d[i] = d_in[i] / dd;
+    for (i = 0; i < 3; i++) {
+        if (d[i] < 0.0) {
+            o[i] = t->size[i] - o[i];
+            d[i] = -d[i];
+            a |= bmask;
+        }
+        bmask >>= 1;
+    }
+    for (i = 0; i < 3; i++) {
+        t0[i] = (t->dle[i] - o[i]) / d[i];
+        t1[i] = (t->dre[i] - o[i]) / d[i];
+    }
+    tmax0 = t0[0];  /* std::max_element: the first largest */
+    for (i = 1; i < 3; i++) if (tmax0 < t0[i]) tmax0 = t0[i];
+    tmin1 = t1[0];  /* std::min_element: the first smallest */
+    for (i = 1; i < 3; i++) if (t1[i] < tmin1) tmin1 = t1[i];
+    if (tmax0 < tmin1) yo_proc_subtree(t, t0[0], t0[1], t0[2], t1[0], t1[1], t1[2], 0, a, fn, ctx);
+}
+
+typedef struct {
+    const yo_sampler *s;
+    const double *cells;  /* 14 per cell: 8 vertex values, left edge, right edge */
+    const double *v_pos, *v_dir;
+    double len;
+    yo_acc *acc;
+    yo_sample_fn fn;
+    int64_t visits;
+    /* trace mode */
+    uint64_t h;
+    int64_t count;
+} yo_octx;
+
+static void yo_octree_cell(void *vctx, int32_t key, double t_in, double t_out)
+{
+    yo_octx *c = (yo_octx *)vctx;
+    yo_vc vc;
+    int k;
+    uint8_t mask[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+    int index[3] = {0, 0, 0};
+    const double *cd = c->cells + 14 * (int64_t)key;
+    vc.n_fields = 1;
+    vc.data[0] = cd;
+    vc.mask = mask;
+    for (k = 0; k < 3; k++) {
+        vc.dims[k] = 1;
+        vc.left_edge[k] = cd[8 + k];
+        vc.right_edge[k] = cd[11 + k];
+        vc.dds[k] = (vc.right_edge[k] - vc.left_edge[k]);
+        vc.idds[k] = 1 / vc.dds[k];
+    }
+    c->visits++;
+    if (c->fn) {
+        c->fn(&vc, c->v_pos, c->v_dir, t_in / c->len, t_out / c->len, index, c->acc);
+    } else {
+        double e = t_in / c->len, x = t_out / c->len;
+        uint64_t eb, xb;
+        memcpy(&eb, &e, 8);
+        memcpy(&xb, &x, 8);
+        c->h = fnv_mix(c->h, (uint64_t)(uint32_t)key);
+        c->h = fnv_mix(c->h, eb);
+        c->h = fnv_mix(c->h, xb);
+        c->count++;
+    }
+}
+
+/* cast_through_octree over the per-pixel rays of s (lens 1); returns the
+ * number of cells sampled.  With hashes/counts set, records per pixel an
+ * FNV-1a hash over (cell key, enter bits, exit bits) instead of sampling. */
+int64_t yo_cast_through_octree(const yo_sampler *s, const double *cells, const void *octree, int num_threads,
+                               uint64_t *hashes, int64_t *counts)
+{
+    const yo_octree *t = (const yo_octree *)octree;
+    int64_t j, size = (int64_t)s->nv[0] * s->nv[1], visits = 0;
+    yo_sample_fn fn = hashes ? NULL : pick_sampler(s->kind);
+    if (s->lens != 1) return -1;
+#ifdef _OPENMP
+    if (num_threads <= 0) num_threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static, 100) num_threads(num_threads) reduction(+ : visits)
+#endif
+    for (j = 0; j < size; j++) {
+        int64_t vj = j % s->nv[1];
+        int64_t vi = (j - vj) / s->nv[1];
+        const double *vp = s->vp_pos + (vi * s->nv[1] + vj) * 3;
+        const double *vd = s->vp_dir + (vi * s->nv[1] + vj) * 3;
+        yo_acc acc;
+        yo_octx c;
+        double *px = s->image + (vi * s->nv[1] + vj) * 4;
+        int k;
+        c.s = s;
+        c.cells = cells;
+        c.v_pos = vp;
+        c.v_dir = vd;
+        c.len = sqrt(pow(vd[0], 2.0) + pow(vd[1], 2.0) + pow(vd[2], 2.0));
+        c.acc = &acc;
+        c.fn = fn;
+        c.visits = 0;
+        c.h = hashes ? hashes[j] : 0;
+        c.count = 0;
+        for (k = 0; k < 4; k++) acc.rgba[k] = px[k];
+        acc.s = s;
+        yo_octree_cast_ray(t, vp, vd, yo_octree_cell, &c);
+        if (c.visits > 0 && !hashes)
+            for (k = 0; k < 4; k++) px[k] = acc.rgba[k];
+        if (hashes) {
+            hashes[j] = c.h;
+            counts[j] += c.count;
+        }
+        visits += c.visits;
+    }
+    (void)num_threads;
+    return visits;
+}

@@ -19,6 +19,9 @@ tests do not depend on the synthetic generators staying bit-stable.
                 perspective), n_samples 1 and 3
 * light.npz     LightSourceRenderSampler images on the vr.npz brick: three
                 cameras x two lights (n_samples 1 and 3) x grey opacity {0,1}
+* octree.npz    cast_through_octree with the reference's _OctreeRayTracing on a
+                ~1500-cell octree: VolumeRenderSampler (1 and 2 samples),
+                ProjectionSampler, InterpolatedProjectionSampler
 * proj.npz      ProjectionSampler (cell-centred) and
                 InterpolatedProjectionSampler (vertex-centred) images
 * kd.npz        AMRKDTree leaves and viewpoint orders (amr_kdtools.pyx
@@ -156,6 +159,49 @@ def light():
     np.savez_compressed(HERE / "light.npz", **out)
 
 
+def octree():
+    """cast_through_octree (image_samplers.pyx:202-288) with the reference's
+    _OctreeRayTracing (_octree_raytracing.hpp): a ~1500-cell octree (levels
+    2-5) through a perspective camera (the octree path reads per-pixel ray
+    arrays), VolumeRenderSampler with 1 and 2 samples, ProjectionSampler and
+    InterpolatedProjectionSampler."""
+    from yt.utilities.lib._octree_raytracing import _OctreeRayTracing
+
+    depth, ipos, lvl, cells = testing.octree_cells(base_level=2, max_level=5, seed=2)
+    key = np.arange(ipos.shape[0], dtype=np.int32)
+    le, re = np.zeros(3), np.ones(3)
+    oc = _OctreeRayTracing(le, re, depth)
+    oc.add_nodes(ipos, lvl, key)
+    vmin, vmax = float(cells[:, :8].min()), float(cells[:, :8].max())
+    layers = testing.ctf_layers((vmin, vmax), 4)
+    tf = glue.color_tf_from_layers((vmin, vmax), 64, layers)
+    out = {"depth": depth, "ipos": ipos, "lvl": lvl, "cells": cells, "tf_y": np.array([t.y for t in tf.tables]),
+           "tf_bounds": np.array((vmin, vmax))}
+    dt = cells.reshape(1, -1, 14, 1)
+    pg = PartitionedGrid(0, dt, np.ones(dt.shape[1:], dtype=np.uint8), le, re, np.array([1, 1, 1], dtype="int64"),
+                         n_fields=1)
+    cam = glue.Camera((0.3, 1.45, -0.9), (0.5, 0.5, 0.5), (1.3, 1.3, 1.3), (26, 22), lens_type="perspective")
+    for name, make in (("vr1", lambda p: RIS.VolumeRenderSampler(*sampler_args_oct(p), tf, 1, **lens_kw(p))),
+                       ("vr2", lambda p: RIS.VolumeRenderSampler(*sampler_args_oct(p), tf, 2, **lens_kw(p))),
+                       ("proj", lambda p: RIS.ProjectionSampler(*sampler_args_oct(p), **lens_kw(p))),
+                       ("iproj", lambda p: RIS.InterpolatedProjectionSampler(*sampler_args_oct(p), 2,
+                                                                             **lens_kw(p)))):
+        p = cam.sampler_params()
+        s = make(p)
+        s(pg, oct=oc)
+        out[f"img_{name}"] = np.array(s.aimage)
+    np.savez_compressed(HERE / "octree.npz", **out)
+
+
+def sampler_args_oct(p):
+    return (p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"], p["x_vec"], p["y_vec"], p["width"],
+            "Octree")
+
+
+def lens_kw(p):
+    return {"lens_type": p["lens_type"], "camera_data": p["camera_data"], "zbuffer": np.ones(p["image"].shape[:2])}
+
+
 def proj():
     rng = np.random.default_rng(13)
     cell = np.exp(rng.standard_normal((12, 12, 12)))
@@ -236,6 +282,7 @@ if __name__ == "__main__":
     trace()
     vr()
     light()
+    octree()
     proj()
     kd_and_amr()
     for f in sorted(HERE.glob("*.npz")):

@@ -9,6 +9,7 @@
 #include "ytgb.h"
 #include "ytgb_ray.cuh"
 #include "ytgb_vertex.cuh"
+#include "ytgb_octree.cuh"
 using namespace ytgb;
 
 template <int MODE, int CTF>
@@ -140,4 +141,69 @@ extern "C" void emu_vertex(const double *cells, int n0, int n1, int n2, double *
     for (int i = 0; i <= n0; i++)
         for (int j = 0; j <= n1; j++)
             for (int k = 0; k <= n2; k++) out[t++] = ytgb::vertex_value(cells, n0, n1, n2, i, j, k);
+}
+
+// cast_through_octree per pixel, as the octree kernel runs it
+// (ytgb_octree.cuh:octree_ray), on the CPU.
+template <int MODE, int CTF>
+static int run_octree(const ytgb_render_args &a, const ytgb_octree_args &oa, unsigned long long *hashes,
+                      long long *counts, unsigned long long *cnt) {
+    std::vector<float4> tab;
+    if (MODE == MODE_VR || MODE == MODE_LIGHT) {
+        const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
+        int nb = a.tf.nbins_max;
+        if (CTF) {
+            tab.resize(3 * nb);
+            for (int b = 0; b < nb; b++) {
+                float4 t0 = g[b], t1 = g[nb + b], t2 = g[2 * nb + b], t3 = g[3 * nb + b];
+                tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
+                tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
+                tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
+            }
+        } else {
+            tab.assign(g, g + a.tf.n_fits * nb);
+        }
+    }
+    OctreeView o;
+    o.nodes = reinterpret_cast<const ONode *>(oa.nodes);
+    o.n_nodes = oa.n_nodes;
+    o.verts = oa.verts;
+    o.edges = oa.edges;
+    o.n_cells = oa.n_cells;
+    o.depth = oa.depth;
+    for (int i = 0; i < 3; i++) {
+        o.dle[i] = oa.dle[i];
+        o.dre[i] = oa.dre[i];
+        o.size[i] = oa.dre[i] - oa.dle[i];
+    }
+    int bad = 0;
+    for (int vi = 0; vi < a.view.nx; vi++)
+        for (int vj = 0; vj < a.view.ny; vj++) {
+            size_t p = (size_t)vi * a.view.ny + vj;
+            Ray r;
+            make_ray(a.view, vi, vj, r);
+            double *img = a.image ? a.image + p * 4 : nullptr;
+            RayState st;
+            ray_state_init(st, MODE != MODE_TRACE ? img : nullptr, 1.0, false, a.flags);
+            unsigned long long th = MODE == MODE_TRACE ? hashes[p] : 0ull;
+            long long tc = 0;
+            if (!octree_ray<MODE, CTF>(a, o, tab.data(), r, st, th, tc)) bad++;
+            if (MODE == MODE_TRACE) { hashes[p] = th; counts[p] += tc; }
+            else for (int c = 0; c < 4; c++) if (st.touched & (1u << c)) img[c] = (double)st.xh[c] + (double)st.xl[c];
+            cnt[0] += st.visits; cnt[1] += st.walks; cnt[3] += st.guarded; cnt[2]++;
+        }
+    return bad;
+}
+
+extern "C" int emu_octree(const ytgb_render_args *a, const ytgb_octree_args *o, int trace,
+                          unsigned long long *hashes, long long *counts, unsigned long long *cnt) {
+    if (trace) return run_octree<MODE_TRACE, 0>(*a, *o, hashes, counts, cnt);
+    switch (a->kind) {
+    case YTGB_VOLUME_RENDER:
+        return a->tf.ctf_fast ? run_octree<MODE_VR, 1>(*a, *o, 0, 0, cnt) : run_octree<MODE_VR, 0>(*a, *o, 0, 0, cnt);
+    case YTGB_PROJECTION: return run_octree<MODE_PROJ, 0>(*a, *o, 0, 0, cnt);
+    case YTGB_INTERPOLATED_PROJECTION: return run_octree<MODE_IPROJ, 0>(*a, *o, 0, 0, cnt);
+    case YTGB_LIGHT_SOURCE: return run_octree<MODE_LIGHT, 0>(*a, *o, 0, 0, cnt);
+    default: return run_octree<MODE_MIP, 0>(*a, *o, 0, 0, cnt);
+    }
 }

@@ -36,6 +36,7 @@ def emu():
     src = HERE / "harness.cpp"
     out = HERE / "_build" / "libytgb_host_walk.so"
     deps = [src, ROOT / "yt_gb300" / "csrc" / "ytgb_ray.cuh", ROOT / "yt_gb300" / "csrc" / "ytgb_vertex.cuh",
+            ROOT / "yt_gb300" / "csrc" / "ytgb_octree.cuh",
             ROOT / "include" / "ytgb.h",
             ROOT / "yt_gb300" / "csrc" / "ytgb_internal.h"]
     if not out.exists() or out.stat().st_mtime < max(d.stat().st_mtime for d in deps):
@@ -297,3 +298,86 @@ def test_light_source_amr(emu):
     w = workloads.amr_vr(root=32, levels=2, patch=8, res=40)
     cam = w.views[0].camera
     check(emu, w.bricks, cam, w.order(cam), _lib.LIGHT_SOURCE, tf=w.tf, light=LIGHT_CASES[1])
+
+
+def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None):
+    """The octree path on the CPU harness and on the oracle, same inputs."""
+    from yt_gb300.octree import ONODE_DTYPE, Octree
+
+    depth, ipos, lvl, cells = testing.octree_cells(base_level=2, max_level=5, seed=seed)
+    oc = Octree(np.zeros(3), np.ones(3), depth)
+    oc.add_nodes(ipos, lvl, np.arange(ipos.shape[0], dtype=np.int32))
+    nodes = oc.nodes()
+    verts = np.ascontiguousarray(cells[:, :8].astype(np.float32))
+    le, re = cells[:, 8:11], cells[:, 11:14]
+    edges = np.ascontiguousarray(np.concatenate([le, re, 1 / (re - le)], axis=1))
+    o = _lib.OctreeArgs()
+    o.nodes, o.verts, o.edges = nodes.ctypes.data, verts.ctypes.data, edges.ctypes.data
+    o.n_nodes, o.n_cells, o.depth = nodes.size, cells.shape[0], depth
+    for i in range(3):
+        o.dle[i], o.dre[i] = 0.0, 1.0
+    p = cam.sampler_params()
+    nx, ny = cam.resolution
+    view, ppos, pdir = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
+                                 p["y_vec"], p["width"], p["lens_type"], p["camera_data"])
+    a = _lib.RenderArgs()
+    a.kind, a.n_samples, a.view = kind, ns, view
+    a.view.px_pos, a.view.px_dir = ppos.ctypes.data, pdir.ctypes.data
+    a.data = verts.ctypes.data
+    keep = []
+    if tf is not None:
+        pk = pack(tf)
+        keep.append(pk)
+        a.tf, a.tf_tables = pk.header, pk.tables.ctypes.data
+    if kind == _lib.LIGHT_SOURCE:
+        from yt_gb300.volume import normalised_light
+
+        ld, rgba = light
+        ld = normalised_light(ld)
+        for i in range(3):
+            a.light_dir[i] = float(ld[i])
+        for i in range(4):
+            a.light_rgba[i] = float(rgba[i])
+    img = np.zeros((nx, ny, 4))
+    a.image = img.ctypes.data
+    cnt = np.zeros(4, dtype=np.uint64)
+    L.emu_octree.argtypes = [C.POINTER(_lib.RenderArgs), C.POINTER(_lib.OctreeArgs), C.c_int, C.c_void_p,
+                             C.c_void_p, C.c_void_p]
+    assert L.emu_octree(C.byref(a), C.byref(o), 0, None, None, cnt.ctypes.data) == 0
+    h = np.full(nx * ny, _lib.FNV_OFFSET, dtype=np.uint64)
+    c = np.zeros(nx * ny, dtype=np.int64)
+    assert L.emu_octree(C.byref(a), C.byref(o), 1, h.ctypes.data, c.ctypes.data,
+                        np.zeros(4, dtype=np.uint64).ctypes.data) == 0
+    # oracle
+    ld, lrgba = light if light is not None else ((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0))
+    ref = np.zeros((nx, ny, 4))
+    s = ocpu.OracleSampler(KN[kind], p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], ref, p["x_vec"],
+                           p["y_vec"], p["width"], lens_type=p["lens_type"], camera_data=p["camera_data"],
+                           n_samples=ns, tf=tf, light_dir=ld, light_rgba=lrgba)
+    oo = ocpu.OracleOctree(depth, np.zeros(3), np.ones(3), ipos, lvl)
+    visits = ocpu.render_octree(s, cells, oo)
+    hr, cr = ocpu.trace_octree(s, cells, oo)
+    return img, cnt, h.reshape(nx, ny), c.reshape(nx, ny), ref, visits, hr, cr, cells
+
+
+@pytest.mark.parametrize("kind", [_lib.VOLUME_RENDER, _lib.PROJECTION, _lib.INTERPOLATED_PROJECTION, _lib.MIP,
+                                  _lib.LIGHT_SOURCE])
+def test_octree_path(emu, kind):
+    """cast_through_octree: traversal (cell keys, enter/exit t bits) bit for
+    bit against the oracle (itself pinned to the compiled reference), images
+    within 1e-5, for every sampler."""
+    cam = Camera((0.3, 1.45, -0.9), (0.5, 0.5, 0.5), (1.3, 1.3, 1.3), (26, 22), lens_type="perspective")
+    tf = None
+    if kind in (_lib.VOLUME_RENDER, _lib.LIGHT_SOURCE):
+        depth, ipos, lvl, cells = testing.octree_cells(base_level=2, max_level=5, seed=2)
+        vmin, vmax = float(cells[:, :8].min()), float(cells[:, :8].max())
+        tf = ColorTransferFunction((vmin, vmax), nbins=64)
+        for loc, wd, rgba in testing.ctf_layers((vmin, vmax), 4):
+            tf.add_gaussian(loc, wd, list(rgba))
+    light = ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0)) if kind == _lib.LIGHT_SOURCE else None
+    for ns in ((1, 2) if kind in (_lib.VOLUME_RENDER, _lib.INTERPOLATED_PROJECTION) else (1,)):
+        img, cnt, h, c, ref, visits, hr, cr, _ = run_octree_both(emu, kind, cam, tf, ns, light=light)
+        assert np.array_equal(c, cr) and np.array_equal(h, hr)
+        assert int(cnt[0]) == visits and visits > 0
+        mx, rms = relative_error(img, ref, channels=(0, 1, 2) if tf is not None else (0,))
+        assert mx <= TOL, f"max relative error {mx:.3e} (rms {rms:.3e})"

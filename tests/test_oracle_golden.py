@@ -167,3 +167,23 @@ def test_light_source_exact(ci, li, grey):
                               light_rgba=lrgba)
     assert visits > 0
     assert np.array_equal(img, f[f"img_{ci}_{li}_{ns}_{grey}"])
+
+
+@pytest.mark.parametrize("name", ["vr1", "vr2", "proj", "iproj"])
+def test_octree_exact(name):
+    """cast_through_octree (image_samplers.pyx:202-288) over the reference's
+    octree ray caster (_octree_raytracing.hpp): oracle == compiled reference,
+    bit for bit."""
+    f = load("octree.npz")
+    oc = ocpu.OracleOctree(int(f["depth"]), np.zeros(3), np.ones(3), f["ipos"], f["lvl"])
+    cam = glue.Camera((0.3, 1.45, -0.9), (0.5, 0.5, 0.5), (1.3, 1.3, 1.3), (26, 22), lens_type="perspective")
+    p = cam.sampler_params()
+    tf = GoldenTF(f["tf_bounds"], f["tf_y"])
+    kind, ns, t = {"vr1": ("volume_render", 1, tf), "vr2": ("volume_render", 2, tf), "proj": ("projection", 1, None),
+                   "iproj": ("interpolated_projection", 2, None)}[name]
+    s = ocpu.OracleSampler(kind, p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"], p["x_vec"],
+                           p["y_vec"], p["width"], lens_type=p["lens_type"], camera_data=p["camera_data"],
+                           n_samples=ns, tf=t)
+    visits = ocpu.render_octree(s, f["cells"], oc)
+    assert visits > 0
+    assert np.array_equal(p["image"], f[f"img_{name}"])

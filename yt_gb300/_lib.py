@@ -111,6 +111,24 @@ class RenderArgs(C.Structure):
     ]
 
 
+class ONode(C.Structure):
+    _fields_ = [("child", C.c_int32 * 8), ("key", C.c_int32), ("flags", C.c_int32)]
+
+
+class OctreeArgs(C.Structure):
+    _fields_ = [
+        ("nodes", C.c_void_p),
+        ("verts", C.c_void_p),
+        ("edges", C.c_void_p),
+        ("n_nodes", C.c_int32),
+        ("n_cells", C.c_int32),
+        ("depth", C.c_int32),
+        ("pad", C.c_int32),
+        ("dle", C.c_double * 3),
+        ("dre", C.c_double * 3),
+    ]
+
+
 class BatchEntry(C.Structure):
     _fields_ = [
         ("args", RenderArgs),
@@ -151,6 +169,13 @@ SIGNATURES = {
                                      C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields_split": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                          C.c_int32]),
+    "ytgb_octree_build": (C.c_void_p, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_int64]),
+    "ytgb_octree_num_nodes": (C.c_int64, [C.c_void_p]),
+    "ytgb_octree_nodes": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ytgb_octree_destroy": (None, [C.c_void_p]),
+    "ytgb_render_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_trace_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                   C.POINTER(C.c_int32)]),

@@ -520,3 +520,81 @@ extern "C" int ytgb_kdtree_viewpoint_orders(void *tree, int32_t n_views, const d
     for (int32_t v = 0; v < n_views; v++) t->viewpoint_order(viewpoints + 3 * v, order + nl * v);
     return YTGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Octree (Octree<int> of _octree_raytracing.hpp, insert_node :139-175 and
+// create_get_node :238-257): nodes numbered in creation order, root first.
+// ---------------------------------------------------------------------------
+namespace {
+struct HostOctree {
+    std::vector<ytgb_onode> nodes;
+    int32_t new_node() {
+        ytgb_onode n;
+        for (int i = 0; i < 8; i++) n.child[i] = -1;
+        n.key = 0;
+        n.flags = 0;
+        nodes.push_back(n);
+        return (int32_t)nodes.size() - 1;
+    }
+};
+}  // namespace
+
+extern "C" void *ytgb_octree_build(int32_t depth, const double *dle, const double *dre, const int32_t *ipos,
+                                   const int32_t *lvl, const int32_t *key, int64_t n) {
+    if (depth < 1 || depth > 30 || n < 0 || (n > 0 && (!ipos || !lvl || !key)) || !dle || !dre) {
+        ytgb_set_error("ytgb_octree_build: bad arguments (depth in [1, 30])");
+        return nullptr;
+    }
+    for (int i = 0; i < 3; i++) {
+        if (!(dre[i] > dle[i])) {
+            ytgb_set_error("ytgb_octree_build: empty domain");
+            return nullptr;
+        }
+    }
+    HostOctree *t = new HostOctree();
+    t->nodes.reserve((size_t)(n > 0 ? n * 2 : 1));
+    t->new_node();
+    for (int64_t c = 0; c < n; c++) {
+        if (lvl[c] < 0 || lvl[c] > depth) {
+            delete t;
+            ytgb_set_error("ytgb_octree_build: cell level outside [0, depth]");
+            return nullptr;
+        }
+        uint64_t mask = (uint64_t)1 << (depth - 1);
+        int32_t node = 0;
+        for (int ibit = depth - 1; ibit >= depth - lvl[c]; --ibit) {
+            int iflat = 0;
+            for (int d = 0; d < 3; d++) {
+                iflat += (((uint64_t)(uint32_t)ipos[3 * c + d]) & mask) != 0;
+                iflat <<= 1;
+            }
+            iflat >>= 1;
+            mask >>= 1;
+            t->nodes[node].flags |= 2;
+            if (t->nodes[node].child[iflat] < 0) {
+                const int32_t nn = t->new_node();
+                t->nodes[node].child[iflat] = nn;
+            }
+            node = t->nodes[node].child[iflat];
+        }
+        t->nodes[node].flags |= 1;
+        t->nodes[node].key = key[c];
+    }
+    return t;
+}
+
+extern "C" int64_t ytgb_octree_num_nodes(void *tree) {
+    return tree ? (int64_t)static_cast<HostOctree *>(tree)->nodes.size() : 0;
+}
+
+extern "C" int ytgb_octree_nodes(void *tree, ytgb_onode *out) {
+    if (!tree || !out) {
+        ytgb_set_error("ytgb_octree_nodes: null argument");
+        return YTGB_ERR_INVALID;
+    }
+    const auto &v = static_cast<HostOctree *>(tree)->nodes;
+    std::memcpy(out, v.data(), v.size() * sizeof(ytgb_onode));
+    return YTGB_OK;
+}
+
+extern "C" void ytgb_octree_destroy(void *tree) { delete static_cast<HostOctree *>(tree); }

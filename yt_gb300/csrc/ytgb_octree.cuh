@@ -1,0 +1,223 @@
+// ytgb_octree.cuh -- the octree ray caster of yt's octree volume source,
+// per ray, host/device (the test harness runs it on the CPU).
+//
+// ImageSampler.cast_through_octree (image_samplers.pyx:202-288) casts each
+// pixel's ray through an octree of cells (Octree<int>::cast_ray,
+// _octree_raytracing.hpp:199-230: the parametric traversal of Revelles,
+// Urena and Lastra, proc_subtree :276-337) and hands every terminal cell it
+// meets, in traversal order, to the sampler as a 1x1x1 vertex-centred brick
+// with the cell's own edges.  The traversal's float64 values (the direction
+// normalisation, the t of the six slab planes, the midpoints) are formed
+// from the same operands in the same order as the reference, unfused, so
+// the cells and their enter/exit t are bit-identical; the recursion becomes
+// an explicit stack of at most depth + 1 frames.
+#pragma once
+
+#include "ytgb_ray.cuh"
+
+namespace ytgb {
+
+// Device form of one octree node: children (-1: none), key, flags.
+struct ONode {
+    int32_t child[8];
+    int32_t key;
+    int32_t flags;  // bit 0: terminal, bit 1: has a children array
+};
+
+struct OctreeView {
+    const ONode *nodes;
+    int32_t n_nodes;
+    const float *verts;    // 8 per cell, (i,j,k) C order
+    const double *edges;   // 9 per cell: left edge, right edge, 1/(right - left)
+    int32_t n_cells;
+    int32_t depth;
+    double dle[3], dre[3], size[3];
+};
+
+constexpr int OCT_MAX_DEPTH = 30;
+
+// std::max / std::min as the reference calls them
+YTGB_HD double smax(double a, double b) { return (a < b) ? b : a; }
+YTGB_HD double smin(double a, double b) { return (b < a) ? b : a; }
+
+YTGB_HD int first_node(double tx0, double ty0, double tz0, double txm, double tym, double tzm) {
+    int index = 0;
+    if (tx0 >= smax(ty0, tz0)) {
+        if (tym < tx0) index |= 2;
+        if (tzm < tx0) index |= 1;
+    } else if (ty0 >= smax(tx0, tz0)) {
+        if (txm < ty0) index |= 4;
+        if (tzm < ty0) index |= 1;
+    } else {
+        if (txm < tz0) index |= 4;
+        if (tym < tz0) index |= 2;
+    }
+    return index;
+}
+
+YTGB_HD int next_node(double tx, double ty, double tz, int ix, int iy, int iz) {
+    if (tx < smin(ty, tz)) return ix;
+    if (ty < smin(tx, tz)) return iy;
+    return iz;
+}
+
+struct OFrame {
+    int32_t node;
+    int32_t inode;  // -1: not entered yet; 8: done
+    double t0[3], t1[3];
+};
+
+// Calls cell(key, t_in, t_out) for every terminal cell of the ray's path,
+// in proc_subtree's order.  Returns false if the stack or step budget ran
+// out (a malformed tree).
+template <typename F>
+YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double d_in[3], F cell) {
+    double p[3], d[3], dd = 0.0, t0[3], t1[3];
+    int a = 0, bmask = 4;
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        p[i] = o_in[i];
+        dd = dadd(dd, dmul(d_in[i], d_in[i]));
+    }
+    dd = dsqrt(dd);
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) d[i] = ddiv(d_in[i], dd);
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        if (d[i] < 0.0) {
+            p[i] = dsub(o.size[i], p[i]);
+            d[i] = -d[i];
+            a |= bmask;
+        }
+        bmask >>= 1;
+    }
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        t0[i] = ddiv(dsub(o.dle[i], p[i]), d[i]);
+        t1[i] = ddiv(dsub(o.dre[i], p[i]), d[i]);
+    }
+    double mx = t0[0], mn = t1[0];  // std::max_element / std::min_element
+    if (mx < t0[1]) mx = t0[1];
+    if (mx < t0[2]) mx = t0[2];
+    if (t1[1] < mn) mn = t1[1];
+    if (t1[2] < mn) mn = t1[2];
+    if (!(mx < mn)) return true;
+    OFrame st[OCT_MAX_DEPTH + 2];
+    int sp = 0;
+    st[0].node = 0;
+    st[0].inode = -1;
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        st[0].t0[i] = t0[i];
+        st[0].t1[i] = t1[i];
+    }
+    const int max_depth = o.depth < OCT_MAX_DEPTH ? o.depth : OCT_MAX_DEPTH;
+    long long budget = 0;
+    while (sp >= 0) {
+        if (++budget > (1LL << 26)) return false;
+        OFrame &f = st[sp];
+        if (f.inode < 0) {
+            // entering proc_subtree
+            if (f.t1[0] < 0 || f.t1[1] < 0 || f.t1[2] < 0 || f.node < 0) {
+                sp--;
+                continue;
+            }
+            if (f.node >= o.n_nodes) return false;
+            const ONode &nd = o.nodes[f.node];
+            const int flags = ldg(&nd.flags);
+            if (flags & 1) {
+                cell(ldg(&nd.key), smax(smax(f.t0[0], f.t0[1]), f.t0[2]), smin(smin(f.t1[0], f.t1[1]), f.t1[2]));
+                sp--;
+                continue;
+            }
+            if (!(flags & 2)) {
+                sp--;
+                continue;
+            }
+            const double xm = dmul(dadd(f.t0[0], f.t1[0]), 0.5), ym = dmul(dadd(f.t0[1], f.t1[1]), 0.5),
+                         zm = dmul(dadd(f.t0[2], f.t1[2]), 0.5);
+            f.inode = first_node(f.t0[0], f.t0[1], f.t0[2], xm, ym, zm);
+        }
+        if (f.inode >= 8) {
+            sp--;
+            continue;
+        }
+        if (sp + 1 > max_depth + 1) return false;
+        const double xm = dmul(dadd(f.t0[0], f.t1[0]), 0.5), ym = dmul(dadd(f.t0[1], f.t1[1]), 0.5),
+                     zm = dmul(dadd(f.t0[2], f.t1[2]), 0.5);
+        // child q's slab: lower or upper half on each axis (bit 2: x, 1: y, 0: z)
+        const int q = f.inode;
+        const bool ux = q & 4, uy = q & 2, uz = q & 1;
+        OFrame &c = st[sp + 1];
+        c.t0[0] = ux ? xm : f.t0[0];
+        c.t1[0] = ux ? f.t1[0] : xm;
+        c.t0[1] = uy ? ym : f.t0[1];
+        c.t1[1] = uy ? f.t1[1] : ym;
+        c.t0[2] = uz ? zm : f.t0[2];
+        c.t1[2] = uz ? f.t1[2] : zm;
+        c.node = ldg(&o.nodes[f.node].child[q ^ a]);
+        c.inode = -1;
+        // the successor among the children (next_node's exit-plane table)
+        switch (q) {
+        case 0: f.inode = next_node(xm, ym, zm, 4, 2, 1); break;
+        case 1: f.inode = next_node(xm, ym, f.t1[2], 5, 3, 8); break;
+        case 2: f.inode = next_node(xm, f.t1[1], zm, 6, 8, 3); break;
+        case 3: f.inode = next_node(xm, f.t1[1], f.t1[2], 7, 8, 8); break;
+        case 4: f.inode = next_node(f.t1[0], ym, zm, 8, 6, 5); break;
+        case 5: f.inode = next_node(f.t1[0], ym, f.t1[2], 8, 7, 8); break;
+        case 6: f.inode = next_node(f.t1[0], f.t1[1], zm, 8, 8, 7); break;
+        default: f.inode = 8; break;
+        }
+        sp++;
+    }
+    return true;
+}
+
+// One pixel of cast_through_octree: the ray cast through the octree and
+// each terminal cell handed to sample_cell as a 1x1x1 brick (dims 1, vertex
+// strides 4 and 2, no mask, one field), with enter/exit t divided by the
+// direction's length (image_samplers.pyx:245-283).  In MODE_TRACE it hashes
+// (key, enter bits, exit bits) into th instead.  Returns false when the
+// traversal gave up (malformed tree).
+template <int MODE, int CTF>
+YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const float4 *s_tab, const Ray &r,
+                        RayState &st, unsigned long long &th, long long &tcount) {
+    const double len = dsqrt(dadd(dadd(dmul(r.dir[0], r.dir[0]), dmul(r.dir[1], r.dir[1])), dmul(r.dir[2], r.dir[2])));
+    return octree_cast(o, r.pos, r.dir, [&](int key, double t_in, double t_out) {
+        if (key < 0 || key >= o.n_cells) {
+            st.guarded++;
+            return;
+        }
+        const double e = ddiv(t_in, len), x = ddiv(t_out, len);
+        if (MODE == MODE_TRACE) {
+            th = fnv_mix(th, (unsigned long long)(unsigned)key);
+            th = fnv_mix(th, (unsigned long long)dbits(e));
+            th = fnv_mix(th, (unsigned long long)dbits(x));
+            tcount++;
+            st.visits++;
+            return;
+        }
+        const double *ed = o.edges + 9ll * key;
+        CellCtx c;
+        c.base = o.verts + 8ll * key;
+        c.fstride = 0;
+        c.moff = -1;
+        c.nf = 1;
+        c.sx = 4;
+        c.sy = 2;
+        float P[3];
+        YTGB_UNROLL
+        for (int i = 0; i < 3; i++) {
+            c.dims[i] = 1;
+            const double idds = ldg(ed + 6 + i);
+            c.vel[i] = fmul(r.fdir[i], (float)idds);
+            // (enter * v_dir + v_pos - left_edge) * idds (image_samplers.pyx:475-478)
+            P[i] = (float)dmul(dsub(dadd(dmul(e, r.dir[i]), r.pos[i]), ldg(ed + i)), idds);
+        }
+        const int cur[3] = {0, 0, 0};
+        st.walks++;
+        sample_cell<MODE, CTF>(a, s_tab, key, c, cur, P, (float)dsub(x, e), dbits(e), dbits(x), st);
+    });
+}
+
+}  // namespace ytgb

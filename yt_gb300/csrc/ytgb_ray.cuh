@@ -41,6 +41,7 @@ YTGB_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
 YTGB_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
 YTGB_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
 YTGB_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+YTGB_HD double dsqrt(double a) { return __dsqrt_rn(a); }
 YTGB_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
 YTGB_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
 YTGB_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
@@ -56,6 +57,7 @@ YTGB_HD double dadd(double a, double b) { return a + b; }
 YTGB_HD double dsub(double a, double b) { return a - b; }
 YTGB_HD double dmul(double a, double b) { return a * b; }
 YTGB_HD double ddiv(double a, double b) { return a / b; }
+YTGB_HD double dsqrt(double a) { return std::sqrt(a); }
 YTGB_HD float fadd(float a, float b) { return a + b; }
 YTGB_HD float fsub(float a, float b) { return a - b; }
 YTGB_HD float fmul(float a, float b) { return a * b; }

@@ -150,8 +150,7 @@ class ImageSampler:
         if self.volume_method == "KDTree":
             return self.cast_through_kdtree(pg, **kwa)
         elif self.volume_method == "Octree":
-            raise NotImplementedError(
-                'Volume rendering has not been implemented for method: "Octree" in yt_gb300')
+            return self.cast_through_octree(pg, **kwa)
         else:
             raise NotImplementedError(
                 f'Volume rendering has not been implemented for method: "{self.volume_method}"')
@@ -162,6 +161,41 @@ class ImageSampler:
         if len(data) > 6:
             raise ValueError("at most 6 fields per brick are supported")
         self._pending.append(pg)
+        return 0
+
+    def cast_through_octree(self, pg, oct=None, num_threads=0):
+        """ImageSampler.cast_through_octree (image_samplers.pyx:202-288): the
+        octree volume source's one PartitionedGrid (14 values per cell, as
+        render_source.py:667-680 packs them) rendered at once through
+        ``oct``, a :class:`yt_gb300.octree.Octree` (the drop-in for yt's
+        ``_OctreeRayTracing``)."""
+        from .octree import Octree, OctreeVolume, render_octree
+
+        if not isinstance(oct, Octree):
+            raise TypeError("cast_through_octree needs a yt_gb300.octree.Octree (in place of _OctreeRayTracing)")
+        if self._px_pos is None:
+            raise ValueError("the octree path casts per-pixel rays: use a perspective (per-pixel) lens")
+        self.flush()
+        dev = _device()
+        cells = np.asarray(pg.my_data[0], dtype=np.float64).reshape(-1, 14)
+        vol = OctreeVolume(oct, cells, dev)
+        img = self._image
+        if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
+            img = np.ascontiguousarray(img, dtype=np.float64)
+        image_d = torch.from_numpy(img).to(dev)
+        px_pos = torch.from_numpy(self._px_pos).to(dev)
+        px_dir = torch.from_numpy(self._px_dir).to(dev)
+        view = self._view
+        view.px_pos, view.px_dir = px_pos.data_ptr(), px_dir.data_ptr()
+        counters = torch.zeros(4, dtype=torch.int64, device=dev)
+        error = torch.zeros(1, dtype=torch.int32, device=dev)
+        render_octree(vol, view, self.kind, image_d, tf=self._tf(), n_samples=self.n_samples, flags=self.flags,
+                      counters=counters, error=error, light=self._light())
+        stream = torch.cuda.current_stream(dev)
+        _lib.check(_lib.lib().ytgb_check_error(error.data_ptr(), stream.cuda_stream), "octree render")
+        self._image[...] = image_d.cpu().numpy()
+        self.last_counters = counters.cpu().numpy()
+        view.px_pos = view.px_dir = None
         return 0
 
     @property

@@ -164,3 +164,61 @@ def ctf_layers(x_bounds, n_layers, width=0.01, colormap=None):
         r, g, b, _ = cmap(rel)
         out.append((float(v), float(width), (r, g, b, float(a))))
     return out
+
+
+def blob_point(p: BlobParams, xyz: np.ndarray) -> np.ndarray:
+    """The blob field 1 + sum_k A_k exp(-|x - c_k|^2 / (2 sigma_k^2)) at
+    points (..., 3)."""
+    rho = np.ones(xyz.shape[:-1], dtype=np.float64)
+    for c, s, a in zip(p.centres, p.sigmas, p.amps):
+        r2 = ((xyz - c) ** 2).sum(axis=-1)
+        rho += a * np.exp(-r2 / (2 * s * s))
+    return rho
+
+
+def octree_cells(base_level=3, max_level=6, seed=0, percentile=70.0, log_field=True):
+    """An octree dataset on [0,1]^3 in the form yt's octree volume source
+    gives its sampler (render_source.py:667-680, octree_raytracing.py:19-41):
+    leaf cells from level ``base_level`` down to ``max_level``, a cell refined
+    where the blob field at its centre exceeds the ``percentile`` of its
+    level.  Returns (depth, ipos (n,3) int32, lvl (n,) int32, cells (n,14)
+    float64: the 8 corner values in (i,j,k) C order, left edge, right edge).
+    ``ipos = floor(centre * 2^depth)`` as the reference computes it."""
+    rng = np.random.default_rng(seed)
+    p = blob_params(rng)
+    depth = max_level
+    n0 = 1 << base_level
+    idx = np.stack(np.meshgrid(*[np.arange(n0)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    level = base_level
+    leaves = []
+    while True:
+        dx = 1.0 / (1 << level)
+        centres = (idx + 0.5) * dx
+        val = blob_point(p, centres)
+        if level < max_level:
+            refine = val > np.percentile(val, percentile)
+        else:
+            refine = np.zeros(val.size, dtype=bool)
+        leaves.append((idx[~refine], level))
+        if not refine.any():
+            break
+        kids = (2 * idx[refine])[:, None, :] + np.stack(np.meshgrid(*[np.arange(2)] * 3, indexing="ij"),
+                                                       -1).reshape(1, 8, 3)
+        idx = kids.reshape(-1, 3)
+        level += 1
+    ipos, lvl, cells = [], [], []
+    for ix, lv in leaves:
+        dx = 1.0 / (1 << lv)
+        le = ix * dx
+        re = le + dx
+        corner = np.stack(np.meshgrid(*[np.arange(2)] * 3, indexing="ij"), -1).reshape(8, 3)
+        pts = le[:, None, :] + corner[None, :, :] * dx
+        v = blob_point(p, pts)
+        if log_field:
+            v = np.log10(v)
+        centre = (ix + 0.5) * dx
+        ipos.append(np.floor(centre * (1 << depth)).astype(np.int32))
+        lvl.append(np.full(ix.shape[0], lv, dtype=np.int32))
+        cells.append(np.concatenate([v, le, re], axis=1))
+    return (depth, np.concatenate(ipos), np.concatenate(lvl),
+            np.ascontiguousarray(np.concatenate(cells), dtype=np.float64))
