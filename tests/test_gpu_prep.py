@@ -84,3 +84,20 @@ def test_device_bricks_reject_bad_slices(cuda):
                               C.c_void_p(s.cuda_stream), None)
     assert st == _lib.OK
     assert L.ytgb_check_error(err.data_ptr(), C.c_void_p(s.cuda_stream)) == _lib.ERR_DEVICE
+
+
+def test_device_bricks_low_parts(cuda):
+    """The low parts (each value's float32 rounding error) written by the
+    device preparation equal the host split packing's."""
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=3)
+    kd = AMRKDTree(grids, log_field=False)
+    host = BrickSet(kd.bricks(), device=cuda, with_lo=True)
+    dev = kd.device_brickset(cuda, with_lo=True)
+
+    def valid_lo(bs):
+        arena = bs.data_lo.cpu().numpy()
+        off = bs.desc_host["data_offset"][: bs.n]
+        return np.concatenate([arena[o: o + v] for o, v in zip(off, bs.verts[: bs.n])])
+
+    assert np.array_equal(valid(dev).view(np.int32), valid(host).view(np.int32))
+    assert np.array_equal(valid_lo(dev).view(np.int32), valid_lo(host).view(np.int32))

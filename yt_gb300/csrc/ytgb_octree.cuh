@@ -216,7 +216,7 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
         }
         const int cur[3] = {0, 0, 0};
         st.walks++;
-        sample_cell<MODE, CTF>(a, s_tab, key, c, cur, P, (float)dsub(x, e), dbits(e), dbits(x), st);
+        sample_cell<MODE, CTF, false>(a, s_tab, key, c, cur, P, (float)dsub(x, e), dbits(e), dbits(x), st);
     });
 }
 

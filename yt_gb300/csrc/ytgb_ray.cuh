@@ -705,7 +705,16 @@ struct CellCtx {
     float vel[3];
 };
 
-template <int MODE, int CTF>
+// The sample position inside the cell, kept in [0, 1] (CLAMP: the walk's
+// cells contain the ray, so only float32 rounding can step outside) or
+// extrapolated as the reference does (the octree path, whose traversal can
+// hand the sampler cells the ray only grazes, with exit_t < enter_t).
+template <bool CLAMP>
+YTGB_HD float cell_coord(float x) {
+    return CLAMP ? fminf(fmaxf(x, 0.0f), 1.0f) : x;
+}
+
+template <int MODE, int CTF, bool CLAMP = true>
 YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi, const CellCtx &c, const int cur[3],
                          const float P[3], float dtf, long long enter_bits, long long exit_bits, RayState &st) {
     st.visits++;
@@ -737,9 +746,9 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
         const float *lo = a.data_lo ? a.data_lo + (c.base - a.data) + off : nullptr;
         for (int s = 0; s < ns; s++) {
             const float f = fmul(dts, (float)s + 0.5f);
-            const float fx = fminf(fmaxf(ffma(f, c.vel[0], P[0]), 0.0f), 1.0f);
-            const float fy = fminf(fmaxf(ffma(f, c.vel[1], P[1]), 0.0f), 1.0f);
-            const float fz = fminf(fmaxf(ffma(f, c.vel[2], P[2]), 0.0f), 1.0f);
+            const float fx = cell_coord<CLAMP>(ffma(f, c.vel[0], P[0]));
+            const float fy = cell_coord<CLAMP>(ffma(f, c.vel[1], P[1]));
+            const float fz = cell_coord<CLAMP>(ffma(f, c.vel[2], P[2]));
             float dvs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             YTGB_UNROLL
             for (int fi = 0; fi < 6; fi++)
@@ -792,9 +801,9 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
     for (int s = 0; s < ns; s++) {
         // sample s at enter_t + (s + 1/2) dt (image_samplers.pyx:475-487)
         const float f = fmul(dts, (float)s + 0.5f);
-        const float fx = fminf(fmaxf(ffma(f, c.vel[0], P[0]), 0.0f), 1.0f);
-        const float fy = fminf(fmaxf(ffma(f, c.vel[1], P[1]), 0.0f), 1.0f);
-        const float fz = fminf(fmaxf(ffma(f, c.vel[2], P[2]), 0.0f), 1.0f);
+        const float fx = cell_coord<CLAMP>(ffma(f, c.vel[0], P[0]));
+        const float fy = cell_coord<CLAMP>(ffma(f, c.vel[1], P[1]));
+        const float fz = cell_coord<CLAMP>(ffma(f, c.vel[2], P[2]));
         if (MODE == MODE_VR && CTF) {
             const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
             const ytgb_tf &tf = a.tf;
