@@ -71,3 +71,30 @@ def test_budget_admission_and_latency(cuda):
     assert s["p99_ms"] >= s["p50_ms"] > 0
     for q in done:
         assert q.admitted >= q.arrival - 1e-9 and q.launched >= q.admitted and q.done >= q.launched
+
+
+def test_cancellation_and_slow_producer(cuda):
+    """Requests cancelled while waiting are dropped without rendering and
+    release their budget; a stalled loop turn (a simulated slow host) delays
+    but does not lose requests."""
+    import time as _time
+
+    srv, _, _ = make_server(cuda, hbm_budget=2 * 48 * 48 * 32, slots=1, max_batch=2)
+    reqs = requests(16, seed=4, rate=5000.0)
+    state = {"turns": 0}
+
+    def tick(server, now):
+        state["turns"] += 1
+        if state["turns"] == 3:
+            for q in reqs[8:12]:
+                q.cancelled = True
+        if state["turns"] == 5:
+            _time.sleep(0.02)
+
+    srv.on_tick = tick
+    done = srv.run(reqs, realtime=True)
+    cancelled = {q.rid for q in srv.cancelled}
+    assert {q.rid for q in done} | cancelled == {q.rid for q in reqs}
+    assert not ({q.rid for q in done} & cancelled)
+    assert srv.in_use == 0
+    assert all(q.image is None for q in srv.cancelled)

@@ -64,7 +64,7 @@ YTGB_HD int next_node(double tx, double ty, double tz, int ix, int iy, int iz) {
 struct OFrame {
     int32_t node;
     int32_t inode;  // -1: not entered yet; 8: done
-    double t0[3], t1[3];
+    double t0[3], t1[3], tm[3];  // tm: the midpoints, once entered
 };
 
 // Calls cell(key, t_in, t_out) for every terminal cell of the ray's path,
@@ -103,60 +103,58 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
     if (t1[2] < mn) mn = t1[2];
     if (!(mx < mn)) return true;
     OFrame st[OCT_MAX_DEPTH + 2];
-    int sp = 0;
-    st[0].node = 0;
-    st[0].inode = -1;
-    YTGB_UNROLL
-    for (int i = 0; i < 3; i++) {
-        st[0].t0[i] = t0[i];
-        st[0].t1[i] = t1[i];
-    }
+    int sp = -1;
     const int max_depth = o.depth < OCT_MAX_DEPTH ? o.depth : OCT_MAX_DEPTH;
+    bool ok = true;
+    // proc_subtree's entry for node n over the slab [c0, c1]: a terminal
+    // node is handed to the sampler at once, an internal one is pushed
+    auto visit = [&](int n, const double c0[3], const double c1[3]) {
+        if (c1[0] < 0 || c1[1] < 0 || c1[2] < 0 || n < 0) return;
+        if (n >= o.n_nodes) {
+            ok = false;
+            return;
+        }
+        const int flags = ldg(&o.nodes[n].flags);
+        if (flags & 1) {
+            cell(ldg(&o.nodes[n].key), smax(smax(c0[0], c0[1]), c0[2]), smin(smin(c1[0], c1[1]), c1[2]));
+            return;
+        }
+        if (!(flags & 2)) return;
+        if (sp + 1 > max_depth) {
+            ok = false;
+            return;
+        }
+        OFrame &f = st[++sp];
+        f.node = n;
+        YTGB_UNROLL
+        for (int i = 0; i < 3; i++) {
+            f.t0[i] = c0[i];
+            f.t1[i] = c1[i];
+            f.tm[i] = dmul(dadd(c0[i], c1[i]), 0.5);
+        }
+        f.inode = first_node(c0[0], c0[1], c0[2], f.tm[0], f.tm[1], f.tm[2]);
+    };
+    visit(0, t0, t1);
     long long budget = 0;
-    while (sp >= 0) {
+    while (sp >= 0 && ok) {
         if (++budget > (1LL << 26)) return false;
         OFrame &f = st[sp];
-        if (f.inode < 0) {
-            // entering proc_subtree
-            if (f.t1[0] < 0 || f.t1[1] < 0 || f.t1[2] < 0 || f.node < 0) {
-                sp--;
-                continue;
-            }
-            if (f.node >= o.n_nodes) return false;
-            const ONode &nd = o.nodes[f.node];
-            const int flags = ldg(&nd.flags);
-            if (flags & 1) {
-                cell(ldg(&nd.key), smax(smax(f.t0[0], f.t0[1]), f.t0[2]), smin(smin(f.t1[0], f.t1[1]), f.t1[2]));
-                sp--;
-                continue;
-            }
-            if (!(flags & 2)) {
-                sp--;
-                continue;
-            }
-            const double xm = dmul(dadd(f.t0[0], f.t1[0]), 0.5), ym = dmul(dadd(f.t0[1], f.t1[1]), 0.5),
-                         zm = dmul(dadd(f.t0[2], f.t1[2]), 0.5);
-            f.inode = first_node(f.t0[0], f.t0[1], f.t0[2], xm, ym, zm);
-        }
-        if (f.inode >= 8) {
+        const int q = f.inode;
+        if (q >= 8) {
             sp--;
             continue;
         }
-        if (sp + 1 > max_depth + 1) return false;
-        const double xm = dmul(dadd(f.t0[0], f.t1[0]), 0.5), ym = dmul(dadd(f.t0[1], f.t1[1]), 0.5),
-                     zm = dmul(dadd(f.t0[2], f.t1[2]), 0.5);
+        const double xm = f.tm[0], ym = f.tm[1], zm = f.tm[2];
         // child q's slab: lower or upper half on each axis (bit 2: x, 1: y, 0: z)
-        const int q = f.inode;
         const bool ux = q & 4, uy = q & 2, uz = q & 1;
-        OFrame &c = st[sp + 1];
-        c.t0[0] = ux ? xm : f.t0[0];
-        c.t1[0] = ux ? f.t1[0] : xm;
-        c.t0[1] = uy ? ym : f.t0[1];
-        c.t1[1] = uy ? f.t1[1] : ym;
-        c.t0[2] = uz ? zm : f.t0[2];
-        c.t1[2] = uz ? f.t1[2] : zm;
-        c.node = ldg(&o.nodes[f.node].child[q ^ a]);
-        c.inode = -1;
+        double c0[3], c1[3];
+        c0[0] = ux ? xm : f.t0[0];
+        c1[0] = ux ? f.t1[0] : xm;
+        c0[1] = uy ? ym : f.t0[1];
+        c1[1] = uy ? f.t1[1] : ym;
+        c0[2] = uz ? zm : f.t0[2];
+        c1[2] = uz ? f.t1[2] : zm;
+        const int child = ldg(&o.nodes[f.node].child[q ^ a]);
         // the successor among the children (next_node's exit-plane table)
         switch (q) {
         case 0: f.inode = next_node(xm, ym, zm, 4, 2, 1); break;
@@ -168,9 +166,9 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
         case 6: f.inode = next_node(f.t1[0], f.t1[1], zm, 8, 8, 7); break;
         default: f.inode = 8; break;
         }
-        sp++;
+        visit(child, c0, c1);
     }
-    return true;
+    return ok;
 }
 
 // One pixel of cast_through_octree: the ray cast through the octree and
@@ -183,12 +181,17 @@ template <int MODE, int CTF>
 YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const float4 *s_tab, const Ray &r,
                         RayState &st, unsigned long long &th, long long &tcount) {
     const double len = dsqrt(dadd(dadd(dmul(r.dir[0], r.dir[0]), dmul(r.dir[1], r.dir[1])), dmul(r.dir[2], r.dir[2])));
+    // The sampler uses enter/exit t only through float32 quantities (dt and
+    // the in-cell position), so a product with 1/len (within an ulp of the
+    // quotient) serves it; the trace keeps the reference's exact quotients.
+    const double ilen = ddiv(1.0, len);
     return octree_cast(o, r.pos, r.dir, [&](int key, double t_in, double t_out) {
         if (key < 0 || key >= o.n_cells) {
             st.guarded++;
             return;
         }
-        const double e = ddiv(t_in, len), x = ddiv(t_out, len);
+        const double e = MODE == MODE_TRACE ? ddiv(t_in, len) : dmul(t_in, ilen);
+        const double x = MODE == MODE_TRACE ? ddiv(t_out, len) : dmul(t_out, ilen);
         if (MODE == MODE_TRACE) {
             th = fnv_mix(th, (unsigned long long)(unsigned)key);
             th = fnv_mix(th, (unsigned long long)dbits(e));

@@ -13,7 +13,9 @@ over time.  The loop:
   their work overlaps on the device (continuous batching, not a queue in
   front of one stream);
 * **retires** a batch when its completion event fires, frees its images'
-  budget and records each request's latency (completion - arrival).
+  budget and records each request's latency (completion - arrival);
+* **drops** requests cancelled before their launch (``Request.cancelled``),
+  releasing their budget; they are listed in ``server.cancelled``.
 
 Each request's image is exactly what rendering it alone gives (the same
 per-ray code, independent of the batch it lands in).
@@ -46,6 +48,7 @@ class Request:
     done: float = -1.0
     image: torch.Tensor | None = None
     samples: int = 0
+    cancelled: bool = False       # set before launch: the request is dropped, never rendered
 
     @property
     def image_bytes(self) -> int:
@@ -87,6 +90,8 @@ class RenderServer:
         self.tile_shape = tile_shape
         self.keep_images = keep_images
         self.samples = 0
+        self.cancelled = []
+        self.on_tick = None   # test hook: called with (server, now) once per loop turn
 
     def renderer(self, volume: str, tf: str | None) -> Renderer:
         key = (volume, tf)
@@ -129,6 +134,16 @@ class RenderServer:
             now = time.perf_counter() - t0
             if now > timeout:
                 raise TimeoutError("render server: requests not finished in time")
+            # requests cancelled before their launch leave without rendering
+            for q in [q for q in pending if q.cancelled]:
+                pending.remove(q)
+                q.done = now
+                self.cancelled.append(q)
+            for q in [q for q in admitted if q.cancelled]:
+                admitted.remove(q)
+                self.in_use -= q.image_bytes
+                q.done = now
+                self.cancelled.append(q)
             # retire finished batches
             for f in list(inflight):
                 if f.event.query():
@@ -143,6 +158,8 @@ class RenderServer:
                     free.append(f.stream)
                     inflight.remove(f)
                     done += f.requests
+            if self.on_tick is not None:
+                self.on_tick(self, now)
             # admit arrivals within the HBM budget
             while pending and (not realtime or pending[0].arrival <= now):
                 q = pending[0]
