@@ -1037,6 +1037,10 @@ static void yo_octree_cell(void *vctx, int32_t key, double t_in, double t_out)
         uint64_t eb, xb;
         memcpy(&eb, &e, 8);
         memcpy(&xb, &x, 8);
+        /* a NaN enters the hash as one pattern: its sign and payload differ
+         * between x86, Arm and the GPU */
+        if (e != e) eb = 0x7ff8000000000000ull;
+        if (x != x) xb = 0x7ff8000000000000ull;
         c->h = fnv_mix(c->h, (uint64_t)(uint32_t)key);
         c->h = fnv_mix(c->h, eb);
         c->h = fnv_mix(c->h, xb);

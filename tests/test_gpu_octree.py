@@ -84,3 +84,40 @@ def test_octree_drop_in(cuda):
                             camera_data=p2["camera_data"], n_samples=2, tf=tf)
     ocpu.render_octree(so, cells, ocpu.OracleOctree(depth, le, re, ipos, lvl))
     assert relative_error(img, p2["image"], channels=(0, 1, 2))[0] <= 1e-5
+
+
+@pytest.mark.parametrize("kind", [_lib.PROJECTION, _lib.MIP])
+def test_octree_axis_rays(cuda, kind):
+    """Per-pixel rays with zero direction components (infinite slab t, NaN
+    midpoints: the traversal's float64-comparison branch) through the
+    drop-in sampler, and their traversal bit for bit."""
+    from yt_gb300.image_samplers import MIPSampler, ProjectionSampler, make_view
+    from yt_gb300.partitioned_grid import PartitionedGrid
+
+    depth, ipos, lvl, cells, oc, tf = dataset()
+    nx, ny = 40, 36
+    pos, d = testing.axis_rays(nx, ny)
+    cam = Camera((0.3, 1.45, -0.9), (0.5, 0.5, 0.5), (1.3, 1.3, 1.3), (nx, ny), lens_type="perspective")
+    p = cam.sampler_params()
+    le, re = np.zeros(3), np.ones(3)
+    dt = cells.reshape(1, -1, 14, 1)
+    pg = PartitionedGrid(0, dt, np.ones(dt.shape[1:], dtype=np.uint8), le, re, np.array([1, 1, 1]), n_fields=1)
+    cls = ProjectionSampler if kind == _lib.PROJECTION else MIPSampler
+    s = cls(pos, d, p["center"], p["bounds"], np.zeros((nx, ny, 4)), p["x_vec"], p["y_vec"], p["width"], "Octree",
+            lens_type="perspective", camera_data=p["camera_data"])
+    s(pg, oct=oc)
+    img = s.aimage.copy()
+    ref = np.zeros((nx, ny, 4))
+    so = ocpu.OracleSampler(KN[kind], pos, d, p["center"], p["bounds"], ref, p["x_vec"], p["y_vec"], p["width"],
+                            lens_type="perspective", camera_data=p["camera_data"])
+    oo = ocpu.OracleOctree(depth, le, re, ipos, lvl)
+    ocpu.render_octree(so, cells, oo)
+    assert relative_error(img, ref, channels=(0,))[0] <= 1e-5
+    vol = OctreeVolume(oc, cells, cuda)
+    view, ppos, pdir = make_view(pos, d, p["center"], p["bounds"], nx, ny, p["x_vec"], p["y_vec"], p["width"],
+                                 "perspective", p["camera_data"])
+    tp, td = torch.from_numpy(ppos).to(cuda), torch.from_numpy(pdir).to(cuda)
+    view.px_pos, view.px_dir = tp.data_ptr(), td.data_ptr()
+    h, c = trace_octree(vol, view)
+    hr, cr = ocpu.trace_octree(so, cells, oo)
+    assert np.array_equal(c, cr) and np.array_equal(h, hr) and c.sum() > 0

@@ -300,8 +300,9 @@ def test_light_source_amr(emu):
     check(emu, w.bricks, cam, w.order(cam), _lib.LIGHT_SOURCE, tf=w.tf, light=LIGHT_CASES[1])
 
 
-def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None):
-    """The octree path on the CPU harness and on the oracle, same inputs."""
+def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None, rays=None):
+    """The octree path on the CPU harness and on the oracle, same inputs
+    (``rays``: per-pixel (positions, directions) replacing the camera's)."""
     from yt_gb300.octree import ONODE_DTYPE, Octree
 
     depth, ipos, lvl, cells = testing.octree_cells(base_level=2, max_level=5, seed=seed)
@@ -318,6 +319,8 @@ def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None):
         o.dle[i], o.dre[i] = 0.0, 1.0
     p = cam.sampler_params()
     nx, ny = cam.resolution
+    if rays is not None:
+        p["vp_pos"], p["vp_dir"] = rays
     view, ppos, pdir = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
                                  p["y_vec"], p["width"], p["lens_type"], p["camera_data"])
     a = _lib.RenderArgs()
@@ -381,3 +384,15 @@ def test_octree_path(emu, kind):
         assert int(cnt[0]) == visits and visits > 0
         mx, rms = relative_error(img, ref, channels=(0, 1, 2) if tf is not None else (0,))
         assert mx <= TOL, f"max relative error {mx:.3e} (rms {rms:.3e})"
+
+
+@pytest.mark.parametrize("kind", [_lib.PROJECTION, _lib.MIP])
+def test_octree_axis_rays(emu, kind):
+    """Rays with zero direction components (infinite slab t, NaN midpoints)
+    traverse bit for bit as the reference's do."""
+    cam = Camera((0.3, 1.45, -0.9), (0.5, 0.5, 0.5), (1.3, 1.3, 1.3), (24, 20), lens_type="perspective")
+    img, cnt, h, c, ref, visits, hr, cr, _ = run_octree_both(emu, kind, cam, rays=testing.axis_rays(24, 20))
+    assert np.array_equal(c, cr) and np.array_equal(h, hr)
+    assert int(cnt[0]) == visits and visits > 0
+    mx, rms = relative_error(img, ref, channels=(0,))
+    assert mx <= TOL, f"max relative error {mx:.3e} (rms {rms:.3e})"

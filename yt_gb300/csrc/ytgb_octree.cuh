@@ -36,28 +36,40 @@ struct OctreeView {
 
 constexpr int OCT_MAX_DEPTH = 30;
 
-// std::max / std::min as the reference calls them
-YTGB_HD double smax(double a, double b) { return (a < b) ? b : a; }
-YTGB_HD double smin(double a, double b) { return (b < a) ? b : a; }
+// The traversal's comparisons.  With K they run on order-preserving int64
+// keys of the doubles (the integer pipe; GB300's float64 pipe is 1/64 of its
+// float32 rate), which order every finite or infinite value exactly as the
+// float64 comparison does.  They hold while no NaN arises: a ray whose six
+// slab t are all below 2^1023 in magnitude has every midpoint (a + b) * 0.5
+// bounded by them, so it takes K; any other ray (a direction component of 0
+// makes inf and, at a midpoint, NaN) takes the float64 comparisons.
+template <bool K> YTGB_HD bool lt(double a, double b) { return K ? dkey(a) < dkey(b) : a < b; }
+template <bool K> YTGB_HD bool ge(double a, double b) { return K ? !(dkey(a) < dkey(b)) : a >= b; }
 
+// std::max / std::min as the reference calls them
+template <bool K> YTGB_HD double smax(double a, double b) { return lt<K>(a, b) ? b : a; }
+template <bool K> YTGB_HD double smin(double a, double b) { return lt<K>(b, a) ? b : a; }
+
+template <bool K>
 YTGB_HD int first_node(double tx0, double ty0, double tz0, double txm, double tym, double tzm) {
     int index = 0;
-    if (tx0 >= smax(ty0, tz0)) {
-        if (tym < tx0) index |= 2;
-        if (tzm < tx0) index |= 1;
-    } else if (ty0 >= smax(tx0, tz0)) {
-        if (txm < ty0) index |= 4;
-        if (tzm < ty0) index |= 1;
+    if (ge<K>(tx0, smax<K>(ty0, tz0))) {
+        if (lt<K>(tym, tx0)) index |= 2;
+        if (lt<K>(tzm, tx0)) index |= 1;
+    } else if (ge<K>(ty0, smax<K>(tx0, tz0))) {
+        if (lt<K>(txm, ty0)) index |= 4;
+        if (lt<K>(tzm, ty0)) index |= 1;
     } else {
-        if (txm < tz0) index |= 4;
-        if (tym < tz0) index |= 2;
+        if (lt<K>(txm, tz0)) index |= 4;
+        if (lt<K>(tym, tz0)) index |= 2;
     }
     return index;
 }
 
+template <bool K>
 YTGB_HD int next_node(double tx, double ty, double tz, int ix, int iy, int iz) {
-    if (tx < smin(ty, tz)) return ix;
-    if (ty < smin(tx, tz)) return iy;
+    if (lt<K>(tx, smin<K>(ty, tz))) return ix;
+    if (lt<K>(ty, smin<K>(tx, tz))) return iy;
     return iz;
 }
 
@@ -70,6 +82,9 @@ struct OFrame {
 // Calls cell(key, t_in, t_out) for every terminal cell of the ray's path,
 // in proc_subtree's order.  Returns false if the stack or step budget ran
 // out (a malformed tree).
+template <bool K, typename F>
+YTGB_HD bool octree_walk(const OctreeView &o, const double t0[3], const double t1[3], int a, F &cell);
+
 template <typename F>
 YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double d_in[3], F cell) {
     double p[3], d[3], dd = 0.0, t0[3], t1[3];
@@ -102,6 +117,18 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
     if (t1[1] < mn) mn = t1[1];
     if (t1[2] < mn) mn = t1[2];
     if (!(mx < mn)) return true;
+    bool bounded = true;  // exponent field below 0x7fe: |t| < 2^1023
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++)
+        bounded = bounded && (dbits(t0[i]) & 0x7ff0000000000000ll) < 0x7fe0000000000000ll &&
+                  (dbits(t1[i]) & 0x7ff0000000000000ll) < 0x7fe0000000000000ll;
+    return bounded ? octree_walk<true>(o, t0, t1, a, cell) : octree_walk<false>(o, t0, t1, a, cell);
+}
+
+// proc_subtree (_octree_raytracing.hpp:276-337) from the root over the slab
+// [t0, t1], with an explicit stack.
+template <bool K, typename F>
+YTGB_HD bool octree_walk(const OctreeView &o, const double t0[3], const double t1[3], int a, F &cell) {
     OFrame st[OCT_MAX_DEPTH + 2];
     int sp = -1;
     const int max_depth = o.depth < OCT_MAX_DEPTH ? o.depth : OCT_MAX_DEPTH;
@@ -109,14 +136,14 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
     // proc_subtree's entry for node n over the slab [c0, c1]: a terminal
     // node is handed to the sampler at once, an internal one is pushed
     auto visit = [&](int n, const double c0[3], const double c1[3]) {
-        if (c1[0] < 0 || c1[1] < 0 || c1[2] < 0 || n < 0) return;
+        if (lt<K>(c1[0], 0.0) || lt<K>(c1[1], 0.0) || lt<K>(c1[2], 0.0) || n < 0) return;
         if (n >= o.n_nodes) {
             ok = false;
             return;
         }
         const int flags = ldg(&o.nodes[n].flags);
         if (flags & 1) {
-            cell(ldg(&o.nodes[n].key), smax(smax(c0[0], c0[1]), c0[2]), smin(smin(c1[0], c1[1]), c1[2]));
+            cell(ldg(&o.nodes[n].key), smax<K>(smax<K>(c0[0], c0[1]), c0[2]), smin<K>(smin<K>(c1[0], c1[1]), c1[2]));
             return;
         }
         if (!(flags & 2)) return;
@@ -132,7 +159,7 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
             f.t1[i] = c1[i];
             f.tm[i] = dmul(dadd(c0[i], c1[i]), 0.5);
         }
-        f.inode = first_node(c0[0], c0[1], c0[2], f.tm[0], f.tm[1], f.tm[2]);
+        f.inode = first_node<K>(c0[0], c0[1], c0[2], f.tm[0], f.tm[1], f.tm[2]);
     };
     visit(0, t0, t1);
     long long budget = 0;
@@ -157,13 +184,13 @@ YTGB_HD bool octree_cast(const OctreeView &o, const double o_in[3], const double
         const int child = ldg(&o.nodes[f.node].child[q ^ a]);
         // the successor among the children (next_node's exit-plane table)
         switch (q) {
-        case 0: f.inode = next_node(xm, ym, zm, 4, 2, 1); break;
-        case 1: f.inode = next_node(xm, ym, f.t1[2], 5, 3, 8); break;
-        case 2: f.inode = next_node(xm, f.t1[1], zm, 6, 8, 3); break;
-        case 3: f.inode = next_node(xm, f.t1[1], f.t1[2], 7, 8, 8); break;
-        case 4: f.inode = next_node(f.t1[0], ym, zm, 8, 6, 5); break;
-        case 5: f.inode = next_node(f.t1[0], ym, f.t1[2], 8, 7, 8); break;
-        case 6: f.inode = next_node(f.t1[0], f.t1[1], zm, 8, 8, 7); break;
+        case 0: f.inode = next_node<K>(xm, ym, zm, 4, 2, 1); break;
+        case 1: f.inode = next_node<K>(xm, ym, f.t1[2], 5, 3, 8); break;
+        case 2: f.inode = next_node<K>(xm, f.t1[1], zm, 6, 8, 3); break;
+        case 3: f.inode = next_node<K>(xm, f.t1[1], f.t1[2], 7, 8, 8); break;
+        case 4: f.inode = next_node<K>(f.t1[0], ym, zm, 8, 6, 5); break;
+        case 5: f.inode = next_node<K>(f.t1[0], ym, f.t1[2], 8, 7, 8); break;
+        case 6: f.inode = next_node<K>(f.t1[0], f.t1[1], zm, 8, 8, 7); break;
         default: f.inode = 8; break;
         }
         visit(child, c0, c1);
@@ -194,8 +221,11 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
         const double x = MODE == MODE_TRACE ? ddiv(t_out, len) : dmul(t_out, ilen);
         if (MODE == MODE_TRACE) {
             th = fnv_mix(th, (unsigned long long)(unsigned)key);
-            th = fnv_mix(th, (unsigned long long)dbits(e));
-            th = fnv_mix(th, (unsigned long long)dbits(x));
+            // a NaN (rays with zero direction components meet NaN slab
+            // midpoints) enters the hash as one pattern: its sign and payload
+            // differ between the GPU and CPUs
+            th = fnv_mix(th, e != e ? 0x7ff8000000000000ull : (unsigned long long)dbits(e));
+            th = fnv_mix(th, x != x ? 0x7ff8000000000000ull : (unsigned long long)dbits(x));
             tcount++;
             st.visits++;
             return;

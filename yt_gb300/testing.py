@@ -222,3 +222,17 @@ def octree_cells(base_level=3, max_level=6, seed=0, percentile=70.0, log_field=T
         cells.append(np.concatenate([v, le, re], axis=1))
     return (depth, np.concatenate(ipos), np.concatenate(lvl),
             np.ascontiguousarray(np.concatenate(cells), dtype=np.float64))
+
+
+def axis_rays(nx, ny, seed=5):
+    """Per-pixel rays ((nx, ny, 3) positions and directions) whose directions
+    have zero components (axis-aligned and in-plane), some starting exactly
+    on cell faces of [0, 1]^3: their slab t are infinite and their slab
+    midpoints NaN."""
+    rng = np.random.default_rng(seed)
+    dirs = np.array([(0, 0, 1), (0, 1, 0), (1, 0, 0), (0, 0, -1), (-1, 0, 0), (0, 0.6, 0.8), (0.8, 0, -0.6),
+                     (0.6, -0.8, 0), (0.3, 0.5, 0.8)], dtype=np.float64)
+    d = dirs[rng.integers(0, len(dirs), size=(nx, ny))]
+    pos = rng.choice(np.arange(1, 16) / 16.0, size=(nx, ny, 3))
+    pos = pos - 1.5 * d + rng.normal(0, 1e-3, size=(nx, ny, 3)) * (rng.random((nx, ny, 1)) < 0.3)
+    return np.ascontiguousarray(pos), np.ascontiguousarray(d)
