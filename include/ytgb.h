@@ -333,6 +333,39 @@ int ytgb_render_octree(const ytgb_render_args *args, const ytgb_octree_args *o, 
 int ytgb_trace_octree(const ytgb_render_args *args, const ytgb_octree_args *o, unsigned long long *hashes,
                       long long *counts, void *stream);
 
+/* ---- octree off-axis projection (cell splatting) ------------------------- */
+/* The cells of an octree dataset projected along a rotated axis by
+ * splatting (image_utilities.pyx:167-289, add_cells_to_image_offaxis, and
+ * its per-cell _add_cell_to_image_offaxis :46-165, called from
+ * off_axis_projection.py:434-499): every cell stamps the projected depth of
+ * a unit cube, precomputed per resolution level ("stamp", :229-246, by
+ * direct_integrate_cube :321-407), onto the pixels it covers, weighted by
+ * the cell's quantity and weight and dx^3 * Nx * Ny.  Pixel (i, j) is the
+ * element i * nx + j of buffer and buffer_weight (the reference's ij2idx,
+ * :43-44), which for nx == ny is the C-order (nx, ny) image; the reference
+ * writes outside its (nx, ny) buffers when nx > ny, which is rejected. */
+typedef struct ytgb_offaxis_args {
+    const double *xp;        /* (n, 3) cell centres, relative to the image centre, in image widths */
+    const double *dxp;       /* n cell widths, in image widths */
+    const double *qty;       /* n */
+    const double *weight;    /* n */
+    const double *stamp;     /* (max_depth, nsx, nsy): the stamps, 0 where the stamp mask is 0 */
+    double *buffer;          /* nx * ny, accumulated into */
+    double *buffer_weight;   /* nx * ny, accumulated into */
+    double rot[6];           /* rows 0 and 1 of the rotation (the camera's inverse matrix, transposed) */
+    int64_t n;
+    int32_t nx, ny;
+    int32_t nsx, nsy;        /* the stamp's extent: max(npix_min, ceil(2 sqrt(3) max(dxp) nx)), ... */
+    int32_t max_depth;       /* ceil(log2(max(nsx, nsy))) */
+    int32_t pad;
+} ytgb_offaxis_args;
+
+/* Replaces add_cells_to_image_offaxis's cell loop (image_utilities.pyx:
+ * 249-289): accumulates every cell into buffer / buffer_weight on the
+ * device.  All pointers are device pointers; d_error (may be NULL) gets
+ * YTGB_DEVERR_BAD_CELL when a cell's stamp index is out of range. */
+int ytgb_offaxis_cells(const ytgb_offaxis_args *args, int32_t *d_error, void *stream);
+
 /* ---- host: AMR kd-tree --------------------------------------------------- */
 /* Replaces AMRKDTree's Tree.build (amr_kdtree.py:109-118) over
  * amr_kdtools.Node.add_grids / insert_grids / split_grids /

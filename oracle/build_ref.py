@@ -2,7 +2,8 @@
 
 This script compiles yt's hot-path Cython/C++ modules (the sampler path of
 ``yt/utilities/lib``: image_samplers, grid_traversal, partitioned_grid,
-lenses, amr_kdtools, interpolators, _octree_raytracing, fixed_interpolator)
+lenses, amr_kdtools, interpolators, _octree_raytracing, image_utilities,
+fixed_interpolator)
 into importable extension modules under ``oracle/_ref/pkg/``.  Nothing it
 produces is product code: only tests, ``__graft_entry__.smoke`` and the CPU
 baseline of ``bench.py`` load it, as a checker.
@@ -53,6 +54,7 @@ MODULES = [
     "amr_kdtools",
     "interpolators",
     "_octree_raytracing",
+    "image_utilities",
 ]
 # headers / sources the generated C++ includes, staged so that stage 2 can run
 # on a machine without the reference checkout

@@ -338,3 +338,48 @@ def trace_octree(sampler: "OracleSampler", cells: np.ndarray, octree: OracleOctr
     L.yo_cast_through_octree(C.byref(sampler.s), cells.ctypes.data, octree.h, int(num_threads),
                              hashes.ctypes.data, counts.ctypes.data)
     return hashes.reshape(nx, ny), counts.reshape(nx, ny)
+
+
+def _offaxis_lib():
+    L = lib()
+    L.yo_offaxis_extent.restype = None
+    L.yo_offaxis_extent.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.yo_offaxis_stamp.restype = C.c_int
+    L.yo_offaxis_stamp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.yo_add_cells_offaxis.restype = C.c_int
+    L.yo_add_cells_offaxis.argtypes = [C.c_void_p] * 4 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p] + \
+        [C.c_int] * 5 + [C.c_void_p, C.c_void_p]
+    return L
+
+
+def offaxis_stamp(rotation, dx_max, nx, ny, npix_min=4):
+    """The stamps and masks of add_cells_to_image_offaxis
+    (image_utilities.pyx:204-246), (max_depth, nsx, nsy)."""
+    L = _offaxis_lib()
+    ext = np.zeros(3, dtype=np.int32)
+    L.yo_offaxis_extent(float(dx_max), int(nx), int(ny), int(npix_min), ext.ctypes.data)
+    nsx, nsy, max_depth = (int(v) for v in ext)
+    rot = np.ascontiguousarray(rotation, dtype=np.float64).reshape(3, 3)
+    stamp = np.zeros((max_depth, nsx, nsy))
+    mask = np.zeros((max_depth, nsx, nsy), dtype=np.uint8)
+    if L.yo_offaxis_stamp(rot.ctypes.data, nsx, nsy, max_depth, stamp.ctypes.data, mask.ctypes.data) != 0:
+        raise RuntimeError("This should not happen")
+    return stamp, mask
+
+
+def add_cells_to_image_offaxis(*, Xp, dXp, qty, weight, rotation, buffer, buffer_weight, Nx, Ny, Npix_min=4):
+    """add_cells_to_image_offaxis (image_utilities.pyx:167-289), sequential:
+    adds into the (Nx, Ny) float64 buffers in place."""
+    L = _offaxis_lib()
+    Xp = np.ascontiguousarray(Xp, dtype=np.float64).reshape(-1, 3)
+    dXp = np.ascontiguousarray(dXp, dtype=np.float64)
+    qty = np.ascontiguousarray(qty, dtype=np.float64)
+    weight = np.ascontiguousarray(weight, dtype=np.float64)
+    rot = np.ascontiguousarray(rotation, dtype=np.float64).reshape(3, 3)
+    stamp, mask = offaxis_stamp(rot, np.max(dXp), Nx, Ny, Npix_min)
+    max_depth, nsx, nsy = stamp.shape
+    assert buffer.flags.c_contiguous and buffer_weight.flags.c_contiguous
+    if L.yo_add_cells_offaxis(Xp.ctypes.data, dXp.ctypes.data, qty.ctypes.data, weight.ctypes.data, Xp.shape[0],
+                              rot.ctypes.data, stamp.ctypes.data, mask.ctypes.data, nsx, nsy, max_depth, int(Nx),
+                              int(Ny), buffer.ctypes.data, buffer_weight.ctypes.data) != 0:
+        raise ValueError("Nx > Ny: the reference writes outside its buffers")

@@ -1095,3 +1095,213 @@ int64_t yo_cast_through_octree(const yo_sampler *s, const double *cells, const v
     (void)num_threads;
     return visits;
 }
+
+/* ---- octree off-axis projection: cell splatting ---------------------------
+ * add_cells_to_image_offaxis (image_utilities.pyx:167-289) with its stamp
+ * precomputation (direct_integrate_cube :321-407, check_in_parallelogram
+ * :296-318) and per-cell splat (_add_cell_to_image_offaxis :46-165),
+ * restated sequentially: one accumulation buffer instead of one per
+ * thread (the reference's thread buffers are summed in an unspecified
+ * order), and the stamp normalised by a left-to-right sum (numpy's pairwise
+ * sum in the reference; the two agree to a few ulps). */
+
+static double oa_fmax(double a, double b) { return a > b ? a : b; } /* fp_utils.pxd */
+static double oa_fmin(double a, double b) { return a < b ? a : b; }
+static double oa_fclip(double f, double a, double b) { return oa_fmin(oa_fmax(f, a), b); }
+
+static int oa_in_parallelogram(const double PA[2], const double PQ[2], const double PR[2], int sPQ, int sPR,
+                               double out[2])
+{
+    double det = PQ[0] * PR[1] - PQ[1] * PR[0];
+    if (det == 0) return 0;
+    out[0] = -(PA[0] * PQ[1] - PA[1] * PQ[0]) / det;
+    out[1] = (PA[0] * PR[1] - PA[1] * PR[0]) / det;
+    return 0 <= sPQ * out[0] && sPQ * out[0] <= 1 && 0 <= sPR * out[1] && sPR * out[1] <= 1;
+}
+
+/* depth of the unit cube spanned by u, v, w from O at the centres of an
+ * nx x ny grid, into buf/mask rows of length stride; -1 on a single hit */
+static int oa_integrate_cube(const double O[3], const double u[3], const double v[3], const double w[3],
+                             double *buf, uint8_t *mask, int nx, int ny, int stride)
+{
+    double Ob[3], F[2], B[2], nm[2];
+    int i, j, k;
+    for (k = 0; k < 3; k++) Ob[k] = O[k] + u[k] + v[k] + w[k];
+    for (i = 0; i < nx; i++) {
+        double X0 = (i + 0.5) * (1. / nx);
+        F[0] = X0 - O[0];
+        B[0] = X0 - Ob[0];
+        for (j = 0; j < ny; j++) {
+            double X1 = (j + 0.5) * (1. / ny), zmin = INFINITY, zmax = -INFINITY, z;
+            int nhit = 0;
+            F[1] = X1 - O[1];
+            B[1] = X1 - Ob[1];
+#define OA_FACE(PA, P, R, s, Z0, c0, c1)                                                                   \
+    if (oa_in_parallelogram(PA, P, R, s, s, nm)) {                                                         \
+        z = Z0 + nm[0] * c0 + nm[1] * c1;                                                                  \
+        zmin = oa_fmin(z, zmin);                                                                           \
+        zmax = oa_fmax(z, zmax);                                                                           \
+        nhit++;                                                                                            \
+    }
+            OA_FACE(F, v, u, 1, O[2], u[2], v[2])
+            OA_FACE(F, w, v, 1, O[2], v[2], w[2])
+            OA_FACE(F, w, u, 1, O[2], u[2], w[2])
+            OA_FACE(B, v, u, -1, Ob[2], u[2], v[2])
+            OA_FACE(B, w, v, -1, Ob[2], v[2], w[2])
+            OA_FACE(B, w, u, -1, Ob[2], u[2], w[2])
+#undef OA_FACE
+            if (nhit == 1) return -1;
+            if (nhit > 1) {
+                buf[i * stride + j] += zmax - zmin;
+                mask[i * stride + j] = 1;
+            }
+        }
+    }
+    return 0;
+}
+
+/* the stamp's extent (image_utilities.pyx:220-225) */
+void yo_offaxis_extent(double dx_max, int nx, int ny, int npix_min, int32_t out[3])
+{
+    int nsx = (int)ceil(2 * dx_max * sqrt(3) * nx), nsy = (int)ceil(2 * dx_max * sqrt(3) * ny);
+    if (nsx < npix_min) nsx = npix_min;
+    if (nsy < npix_min) nsy = npix_min;
+    out[0] = nsx;
+    out[1] = nsy;
+    out[2] = (int)ceil(log2((double)(nsx > nsy ? nsx : nsy)));
+}
+
+/* the stamps (image_utilities.pyx:204-246) into stamp / mask
+ * (max_depth, nsx, nsy), zeroed by the caller; rot is the 3x3 rotation,
+ * row-major.  Returns -1 where the reference raises. */
+int yo_offaxis_stamp(const double *rot, int nsx, int nsy, int max_depth, double *stamp, uint8_t *mask)
+{
+    double w0 = 1 / sqrt(3.), e[3][3] = {{0}}, abc[3][3], o[3];
+    int i, k, d;
+    for (i = 0; i < 3; i++) e[i][i] = 1. * w0;
+    for (i = 0; i < 3; i++)
+        for (k = 0; k < 3; k++)
+            abc[i][k] = rot[3 * k] * e[i][0] + rot[3 * k + 1] * e[i][1] + rot[3 * k + 2] * e[i][2];
+    for (k = 0; k < 3; k++) o[k] = 0.5 - (abc[0][k] + abc[1][k] + abc[2][k]) / 2;
+    for (d = 0; d < max_depth; d++) {
+        double *s = stamp + (int64_t)d * nsx * nsy, sum = 0;
+        int64_t m;
+        if (d == 0) {
+            s[0] = 1;
+            continue;
+        }
+        if (oa_integrate_cube(o, abc[0], abc[1], abc[2], s, mask + (int64_t)d * nsx * nsy,
+                              (1 << d) < nsx ? (1 << d) : nsx, (1 << d) < nsy ? (1 << d) : nsy, nsy) < 0)
+            return -1;
+        for (m = 0; m < (int64_t)nsx * nsy; m++) sum += s[m];
+        for (m = 0; m < (int64_t)nsx * nsy; m++) s[m] /= sum;
+    }
+    return 0;
+}
+
+static void oa_add(double *b, double *bw, int64_t idx, int64_t npix, double vq, double vw)
+{
+    if (idx >= 0 && idx < npix) {
+        b[idx] += vq;
+        bw[idx] += vw;
+    }
+}
+
+/* _add_cell_to_image_offaxis (image_utilities.pyx:46-165) for one cell into
+ * the linear buffers b / bw (pixel (i, j) at i * nx + j) */
+static void oa_cell(double dx, double w, double q, double cmw, double x, double y, int nx, int ny, int nsx,
+                    int nsy, double *b, double *bw, int max_depth, const double *stamp, const uint8_t *mask)
+{
+    double half = cmw / 2, dx3 = dx * dx * dx * nx * ny, lx = x - half, rx = x + half, ly = y - half,
+           ry = y + half, dx_loc, dy_loc;
+    int64_t npix = (int64_t)nx * ny;
+    int jmin = (int)floor(lx * nx), jmax = (int)ceil(rx * nx), kmin = (int)floor(ly * ny),
+        kmax = (int)ceil(ry * ny), depth, j, k;
+    if (jmin < 0) jmin = 0;
+    if (jmax < nx - 1) jmax = nx - 1;
+    if (kmin > 0) kmin = 0;
+    if (kmax < ny - 1) kmax = ny - 1;
+    if (jmax == jmin + 1 && kmax == kmin + 1) {
+        oa_add(b, bw, (int64_t)jmin * nx + kmin, npix, q * dx3, w * dx3);
+        return;
+    }
+    depth = (int)ceil(log2(4 * sqrt(3) * dx * oa_fmax(nx, ny)));
+    if (depth < 1) depth = 1;
+    if (depth > max_depth - 1) depth = max_depth - 1;
+    jmax = nsx < (1 << depth) ? nsx : (1 << depth);
+    kmax = nsy < (1 << depth) ? nsy : (1 << depth);
+    dx_loc = cmw / jmax;
+    dy_loc = cmw / kmax;
+    for (j = 0; j < jmax; j++) {
+        double xx1 = ((j - jmax / 2.) * dx_loc + x) * nx, xx2 = ((j + 1 - jmax / 2.) * dx_loc + x) * nx, dvx;
+        int jj1 = (int)xx1, jj2 = (int)xx2;
+        if (jj2 < 0 || jj1 >= nx) continue;
+        dvx = oa_fclip((jj2 - xx1) / (xx2 - xx1), 0., 1.);
+        for (k = 0; k < kmax; k++) {
+            int64_t si = ((int64_t)depth * nsx + j) * nsy + k;
+            double yy1, yy2, tmp, sw, sq, dvy;
+            int kk1, kk2;
+            if (mask[si] == 0) continue;
+            yy1 = ((k - kmax / 2.) * dy_loc + y) * ny;
+            yy2 = ((k + 1 - kmax / 2.) * dy_loc + y) * ny;
+            kk1 = (int)yy1;
+            kk2 = (int)yy2;
+            if (kk2 < 0 || kk1 >= ny) continue;
+            tmp = stamp[si] * dx3;
+            sw = tmp * w;
+            sq = tmp * q;
+            dvy = oa_fclip((kk2 - yy1) / (yy2 - yy1), 0., 1.);
+            if (jj1 >= 0 && kk1 >= 0) {
+                tmp = dvx * dvy;
+                oa_add(b, bw, (int64_t)jj1 * nx + kk1, npix, sq * tmp, sw * tmp);
+            }
+            if (jj1 >= 0 && kk2 < ny) {
+                tmp = dvx * (1 - dvy);
+                oa_add(b, bw, (int64_t)jj1 * nx + kk2, npix, sq * tmp, sw * tmp);
+            }
+            if (jj2 < nx && kk1 >= 0) {
+                tmp = (1 - dvx) * dvy;
+                oa_add(b, bw, (int64_t)jj2 * nx + kk1, npix, sq * tmp, sw * tmp);
+            }
+            if (jj2 < nx && kk2 < ny) {
+                tmp = (1 - dvx) * (1 - dvy);
+                oa_add(b, bw, (int64_t)jj2 * nx + kk2, npix, sq * tmp, sw * tmp);
+            }
+        }
+    }
+}
+
+/* The cell loop of add_cells_to_image_offaxis (image_utilities.pyx:249-289):
+ * every cell into a zeroed linear buffer, then buffer[j, k] += linear[j *
+ * nx + k] for the (nx, ny) C-order outputs.  Returns -1 for nx > ny (the
+ * reference then writes outside its buffer) or on allocation failure. */
+int yo_add_cells_offaxis(const double *xp, const double *dxp, const double *qty, const double *weight, int64_t n,
+                         const double *rot, const double *stamp, const uint8_t *mask, int nsx, int nsy,
+                         int max_depth, int nx, int ny, double *buffer, double *buffer_weight)
+{
+    int64_t i, npix = (int64_t)nx * ny;
+    double *lb, *lbw, sq3 = sqrt(3.);
+    int j, k;
+    if (nx > ny) return -1;
+    lb = (double *)calloc((size_t)npix, sizeof(double));
+    lbw = (double *)calloc((size_t)npix, sizeof(double));
+    if (!lb || !lbw) {
+        free(lb);
+        free(lbw);
+        return -1;
+    }
+    for (i = 0; i < n; i++) {
+        double dx = dxp[i], cmw = dx * sq3;
+        double x = (rot[0] * xp[3 * i] + rot[1] * xp[3 * i + 1] + rot[2] * xp[3 * i + 2]) + 0.5;
+        double y = (rot[3] * xp[3 * i] + rot[4] * xp[3 * i + 1] + rot[5] * xp[3 * i + 2]) + 0.5;
+        oa_cell(dx, weight[i], qty[i], cmw, x, y, nx, ny, nsx, nsy, lb, lbw, max_depth, stamp, mask);
+    }
+    for (j = 0; j < nx; j++)
+        for (k = 0; k < ny; k++) {
+            buffer[(int64_t)j * ny + k] += lb[(int64_t)j * nx + k];
+            buffer_weight[(int64_t)j * ny + k] += lbw[(int64_t)j * nx + k];
+        }
+    free(lb);
+    free(lbw);
+    return 0;
+}

@@ -29,6 +29,11 @@ tests do not depend on the synthetic generators staying bit-stable.
 * amr_vr.npz    a full AMR render: bricks from the reference's kd tree and
                 vertex centring, rendered by the reference sampler in
                 viewpoint order through a perspective camera
+* offaxis.npz   add_cells_to_image_offaxis (image_utilities.pyx:167-289):
+                octree cells splatted along oblique normals (offaxis_cases)
+
+Pass fixture names (gz trace vr light octree proj kd offaxis) to make only
+those.
 """
 from __future__ import annotations
 
@@ -277,13 +282,60 @@ def kd_and_amr():
                         tf_bounds=np.array(bounds), viewpoint=cam.viewpoint)
 
 
+def offaxis_cases():
+    """Inputs of offaxis.npz: the cells of a small octree (levels 2-5) seen
+    along oblique normals on square, non-square (Nx < Ny), one- and
+    two-pixel images; the last case adds cells wider than the image (more
+    stamp subcells per row than the device table holds) and cells partly
+    or wholly outside the image.  Returns (base cells, extra cells, views)."""
+    from yt_gb300.camera import Camera
+
+    _, _, _, cells = testing.octree_cells(base_level=2, max_level=5, seed=2)
+    le, re = cells[:, 8:11], cells[:, 11:14]
+    rng = np.random.default_rng(21)
+    base = ((le + re) / 2 - 0.5, np.ascontiguousarray((re - le)[:, 0]), cells[:, :8].mean(axis=1),
+            rng.uniform(0.5, 2.0, cells.shape[0]))
+    bx = np.array([[0.1, -0.2, 0.05], [-0.3, 0.25, 0.0], [0.45, 0.45, -0.1]])
+    extra = (np.concatenate([bx, rng.uniform(-0.8, 0.8, (40, 3))]),
+             np.concatenate([[1.3, 0.6, 0.35], rng.choice([1 / 16, 1 / 32, 1 / 64], 40)]),
+             rng.uniform(0.1, 3, 43), rng.uniform(0.5, 2, 43))
+    views = []
+    for pos, nx, ny, ext in [((0.1, 0.3, -1.2), 40, 40, False), ((1.3, 0.2, 0.4), 32, 56, False),
+                             ((0.5, 0.5, -1.0), 1, 1, False), ((0.2, 0.9, -0.7), 2, 2, False),
+                             ((-0.4, 1.1, 0.3), 120, 120, True)]:
+        cam = Camera(pos, (0.5, 0.5, 0.5), (1, 1, 1), (nx, ny), lens_type="plane-parallel")
+        views.append((np.ascontiguousarray(cam.inv_mat.T), nx, ny, ext))
+    return base, extra, views
+
+
+def offaxis_inputs(base, extra, ext):
+    """The cell arrays of one offaxis.npz case (base cells, plus the extra
+    ones when ext)."""
+    if not ext:
+        return tuple(np.ascontiguousarray(a) for a in base)
+    return tuple(np.ascontiguousarray(np.concatenate([a, b])) for a, b in zip(base, extra))
+
+
+def offaxis():
+    from yt.utilities.lib import image_utilities as RIU
+
+    base, extra, views = offaxis_cases()
+    arrays = {"X": base[0], "D": base[1], "Q": base[2], "W": base[3], "eX": extra[0], "eD": extra[1],
+              "eQ": extra[2], "eW": extra[3]}
+    for i, (rot, nx, ny, ext) in enumerate(views):
+        X, D, Q, W = offaxis_inputs(base, extra, ext)
+        b, bw = np.zeros((nx, ny)), np.zeros((nx, ny))
+        RIU.add_cells_to_image_offaxis(Xp=X, dXp=D, qty=Q, weight=W, rotation=rot, buffer=b, buffer_weight=bw,
+                                       Nx=nx, Ny=ny)
+        arrays.update({f"rot{i}": rot, f"view{i}": np.array([nx, ny, int(ext)]), f"b{i}": b, f"bw{i}": bw})
+    np.savez_compressed(HERE / "offaxis.npz", n=len(views), **arrays)
+
+
+ALL = {"gz": gz, "trace": trace, "vr": vr, "light": light, "octree": octree, "proj": proj, "kd": kd_and_amr,
+       "offaxis": offaxis}
+
 if __name__ == "__main__":
-    gz()
-    trace()
-    vr()
-    light()
-    octree()
-    proj()
-    kd_and_amr()
+    for name in sys.argv[1:] or list(ALL):
+        ALL[name]()
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -1,8 +1,9 @@
 """Pin the oracle to yt's own compiled sampler through the golden fixtures
 (generated by tests/golden/make_golden.py from the reference sources).
 
-Everything here is float64 and bit-exact: the C oracle reproduces yt's
-images, traversal sequences, vertex centring and kd-tree exactly.
+Everything here is float64 and bit-exact -- the C oracle reproduces yt's
+images, traversal sequences, vertex centring and kd-tree exactly -- except
+the off-axis cell splatting, whose reference sums in an unspecified order.
 """
 from pathlib import Path
 
@@ -187,3 +188,42 @@ def test_octree_exact(name):
     visits = ocpu.render_octree(s, f["cells"], oc)
     assert visits > 0
     assert np.array_equal(p["image"], f[f"img_{name}"])
+
+
+def offaxis_case(f, i):
+    """Inputs of case i of offaxis.npz (make_golden.offaxis_inputs)."""
+    nx, ny, ext = (int(v) for v in f[f"view{i}"])
+    cells = [f[k] for k in ("X", "D", "Q", "W")]
+    if ext:
+        cells = [np.ascontiguousarray(np.concatenate([a, f["e" + k]])) for a, k in zip(cells, "XDQW")]
+    return (*cells, f[f"rot{i}"], nx, ny)
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_offaxis_oracle(i):
+    """add_cells_to_image_offaxis: the oracle against the reference's own
+    images.  Both are float64 and differ only in summation order (the
+    reference normalises its stamps with numpy's pairwise sum and adds its
+    per-thread buffers in any order), hence 1e-12 rather than bit-exact."""
+    f = load("offaxis.npz")
+    X, D, Q, W, rot, nx, ny = offaxis_case(f, i)
+    b, bw = np.zeros((nx, ny)), np.zeros((nx, ny))
+    ocpu.add_cells_to_image_offaxis(Xp=X, dXp=D, qty=Q, weight=W, rotation=rot, buffer=b, buffer_weight=bw,
+                                    Nx=nx, Ny=ny)
+    for got, ref in ((b, f[f"b{i}"]), (bw, f[f"bw{i}"])):
+        assert np.max(np.abs(ref)) > 0
+        assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_offaxis_stamp_product_matches_oracle():
+    """The product's host stamps (numpy, the reference's operations) and the
+    oracle's (C): identical masks, values equal up to the normalising sum."""
+    from yt_gb300 import offaxis
+
+    f = load("offaxis.npz")
+    for i in range(int(f["n"])):
+        X, D, Q, W, rot, nx, ny = offaxis_case(f, i)
+        s1, m1 = offaxis.offaxis_stamp(rot, np.max(D), nx, ny)
+        s2, m2 = ocpu.offaxis_stamp(rot, np.max(D), nx, ny)
+        assert s1.shape == s2.shape and np.array_equal(m1, m2)
+        assert np.max(np.abs(s1 - s2)) <= 1e-15

@@ -129,6 +129,26 @@ class OctreeArgs(C.Structure):
     ]
 
 
+class OffaxisArgs(C.Structure):
+    _fields_ = [
+        ("xp", C.c_void_p),
+        ("dxp", C.c_void_p),
+        ("qty", C.c_void_p),
+        ("weight", C.c_void_p),
+        ("stamp", C.c_void_p),
+        ("buffer", C.c_void_p),
+        ("buffer_weight", C.c_void_p),
+        ("rot", C.c_double * 6),
+        ("n", C.c_int64),
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("nsx", C.c_int32),
+        ("nsy", C.c_int32),
+        ("max_depth", C.c_int32),
+        ("pad", C.c_int32),
+    ]
+
+
 class BatchEntry(C.Structure):
     _fields_ = [
         ("args", RenderArgs),
@@ -175,6 +195,7 @@ SIGNATURES = {
     "ytgb_octree_nodes": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ytgb_octree_destroy": (None, [C.c_void_p]),
     "ytgb_render_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_offaxis_cells": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_trace_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,

@@ -24,7 +24,7 @@ OUTDIR = PKG / "lib"
 LIB = OUTDIR / "libytgb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ytgb_render.cu", "ytgb_prep.cu", "ytgb_octree.cu"]
+CU_SOURCES = ["ytgb_render.cu", "ytgb_prep.cu", "ytgb_octree.cu", "ytgb_offaxis.cu"]
 CPP_SOURCES = ["ytgb_host.cpp", "ytgb_pack.cpp"]
 
 

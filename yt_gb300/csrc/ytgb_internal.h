@@ -9,6 +9,7 @@ void ytgb_set_error(const std::string &msg);
 #define YTGB_DEVERR_STEP_LIMIT 1      // a DDA walk exceeded its step bound
 #define YTGB_DEVERR_BAD_BRICK 2       // brick index / dims out of range
 #define YTGB_DEVERR_BAD_TF 3          // transfer function header inconsistent
+#define YTGB_DEVERR_BAD_CELL 4        // an off-axis cell's stamp level out of range
 
 // FNV-1a 64-bit offset basis and prime (traversal trace)
 #define YTGB_FNV_OFFSET 1469598103934665603ull
