@@ -59,19 +59,30 @@ __device__ __forceinline__ double boundary(int i, int m, double d_loc, double x,
     return ytgb::dmul(ytgb::dadd(ytgb::dmul(ytgb::dsub((double)i, (double)m * 0.5), d_loc), x), (double)N);
 }
 
-__device__ __forceinline__ void fill_axis(AxisTable &t, int lane, int m, double d_loc, double x, int N) {
-    for (int i = lane; i <= m; i += 32) {
-        const double b0 = boundary(i, m, d_loc, x, N);
-        const int e0 = __double2int_rz(b0);
-        t.edge[i] = e0;
-        if (i < m) {
-            const double b1 = boundary(i + 1, m, d_loc, x, N);
-            const int e1 = __double2int_rz(b1);
-            const double dv = fclip(ytgb::ddiv(ytgb::dsub((double)e1, b0), ytgb::dsub(b1, b0)), 0.0, 1.0);
-            t.dv[i] = dv;
-            t.uv[i] = ytgb::dsub(1.0, dv);
-        }
-    }
+// Entry i of an axis table: boundaries i and i + 1, their truncations and
+// dv (image_utilities.pyx:110-120 and 124-138); entry m - 1 also stores the
+// last edge.
+__device__ __forceinline__ void fill_entry(AxisTable &t, int i, int m, double d_loc, double x, int N) {
+    const double b0 = boundary(i, m, d_loc, x, N), b1 = boundary(i + 1, m, d_loc, x, N);
+    const int e1 = __double2int_rz(b1);
+    t.edge[i] = __double2int_rz(b0);
+    if (i == m - 1) t.edge[m] = e1;
+    const double dv = fclip(ytgb::ddiv(ytgb::dsub((double)e1, b0), ytgb::dsub(b1, b0)), 0.0, 1.0);
+    t.dv[i] = dv;
+    t.uv[i] = ytgb::dsub(1.0, dv);
+}
+
+// ceil(log2(v)) for finite v > 1 as the C library's log2 gives it: E for
+// v = 2^E exactly, E + 1 when v lies more than 2^12 ulps above 2^E (log2(v)
+// then exceeds E by over ten of its own ulps), and the library log2 in the
+// narrow band between.
+__device__ __forceinline__ int ceil_log2_above1(double v) {
+    const long long b = dbits(v);
+    const int E = (int)(b >> 52) - 1023;
+    const long long f = b & MANT52;
+    if (f == 0) return E;
+    if (f >= 4096) return E + 1;
+    return __double2int_rz(ceil(log2(v)));
 }
 
 // smallest k in [0, m) with edge[k + 1] >= Q (m if none)
@@ -127,7 +138,7 @@ __device__ __forceinline__ void add_to(PixelRun &r, int P, double t, double f, d
 struct Column {
     const double *stamp;  // this depth's stamp
     long long nsy;
-    int klo, Q, nx;
+    int klo, kcap, Q, nx;  // kcap: the last subcell of a row
     long long npix;
     double cq, cw;
     double *buf, *bufw;
@@ -137,18 +148,16 @@ struct Column {
 // stamp[j][k] * fy_k(Q) over the N subcells k = klo .. klo + N - 1 that
 // meet Q (weights w), spread over the row's two pixels with dvx, 1 - dvx.
 template <int N>
-__device__ __forceinline__ void column_rows(const AxisTable &tx, const Column &c, const double *w, int j0, int j1) {
-    double wk[N];
-#pragma unroll
-    for (int u = 0; u < N; u++) wk[u] = w[u];
+__device__ __forceinline__ void column_rows(const AxisTable &tx, const Column &c, const double (&wk)[OA_MAXK], int j0,
+                                            int j1) {
     PixelRun run;
     for (int j = j0; j < j1; j++) {
         const int e0 = tx.edge[j], e1 = tx.edge[j + 1];
         if (e1 < 0 || e0 >= c.nx) continue;  // image_utilities.pyx:116
-        const double *srow = c.stamp + (long long)j * c.nsy + c.klo;
+        const double *srow = c.stamp + (long long)j * c.nsy;
         double t = 0.0;
 #pragma unroll
-        for (int u = 0; u < N; u++) t = __fma_rn(__ldg(srow + u), wk[u], t);
+        for (int u = 0; u < N; u++) t = __fma_rn(__ldg(srow + min(c.klo + u, c.kcap)), wk[u], t);
         if (e0 >= 0) add_to(run, e0, t, tx.dv[j], c.buf, c.bufw, c.Q, c.nx, c.npix, c.cq, c.cw);
         if (e1 < c.nx) add_to(run, e1, t, tx.uv[j], c.buf, c.bufw, c.Q, c.nx, c.npix, c.cq, c.cw);
     }
@@ -229,6 +238,7 @@ __global__ void __launch_bounds__(OA_BLOCK) offaxis_kernel(const ytgb_offaxis_ar
     const int nx = a.nx, ny = a.ny;
     const long long npix = (long long)nx * ny;
     const double sq3 = ytgb::dsqrt(3.0);
+    const double sq3x4 = ytgb::dmul(4.0, sq3);
     const double nmax = nx > ny ? (double)nx : (double)ny;  // fmax(Nx, Ny)
     const long long n_warps = (long long)gridDim.x * OA_WARPS;
     for (long long c = (long long)blockIdx.x * OA_WARPS + wib; c < a.n; c += n_warps) {
@@ -242,7 +252,7 @@ __global__ void __launch_bounds__(OA_BLOCK) offaxis_kernel(const ytgb_offaxis_ar
         const double cmw = ytgb::dmul(dx, sq3);
         const double x = ytgb::dadd(ytgb::dadd(ytgb::dadd(ytgb::dmul(a.rot[0], X0), ytgb::dmul(a.rot[1], X1)), ytgb::dmul(a.rot[2], X2)), 0.5);
         const double y = ytgb::dadd(ytgb::dadd(ytgb::dadd(ytgb::dmul(a.rot[3], X0), ytgb::dmul(a.rot[4], X1)), ytgb::dmul(a.rot[5], X2)), 0.5);
-        const double half = ytgb::ddiv(cmw, 2.0);
+        const double half = ytgb::dmul(cmw, 0.5);  // cmw / 2, exactly
         const double dx3 = ytgb::dmul(ytgb::dmul(ytgb::dmul(ytgb::dmul(dx, dx), dx), (double)nx), (double)ny);
         const double lx = ytgb::dsub(x, half), rx = ytgb::dadd(x, half), ly = ytgb::dsub(y, half), ry = ytgb::dadd(y, half);
         const int jmin = max(__double2int_rz(floor(ytgb::dmul(lx, (double)nx))), 0);
@@ -258,18 +268,24 @@ __global__ void __launch_bounds__(OA_BLOCK) offaxis_kernel(const ytgb_offaxis_ar
             continue;
         }
         // :92-99: the stamp level with at least 4 subcells per pixel diagonal
-        int depth = __double2int_rz(ceil(log2(ytgb::dmul(ytgb::dmul(ytgb::dmul(4.0, sq3), dx), nmax))));
+        const double v = ytgb::dmul(ytgb::dmul(sq3x4, dx), nmax);
+        int depth = v > 1.0 ? ceil_log2_above1(v) : 1;
         depth = depth < 1 ? 1 : (depth > a.max_depth - 1 ? a.max_depth - 1 : depth);
         const int jm = min(a.nsx, 1 << depth), km = min(a.nsy, 1 << depth);
-        const double dx_loc = ytgb::ddiv(cmw, (double)jm), dy_loc = ytgb::ddiv(cmw, (double)km);
+        // cmw / 2^depth is an exact scaling
+        const double pw = dfrom((long long)(1023 - depth) << 52);
+        const double dx_loc = jm == (1 << depth) ? ytgb::dmul(cmw, pw) : ytgb::ddiv(cmw, (double)jm);
+        const double dy_loc = km == (1 << depth) ? ytgb::dmul(cmw, pw) : ytgb::ddiv(cmw, (double)km);
         const double cq = ytgb::dmul(dx3, q), cw = ytgb::dmul(dx3, w);
         if (jm > OA_KT || km > OA_KT) {
             cell_direct(a, lane, depth, jm, km, dx_loc, dy_loc, x, y, dx3, w, q);
             continue;
         }
         __syncwarp();
-        fill_axis(tx, lane, jm, dx_loc, x, nx);
-        fill_axis(ty, lane, km, dy_loc, y, ny);
+        for (int e = lane; e < jm + km; e += 32) {
+            if (e < jm) fill_entry(tx, e, jm, dx_loc, x, nx);
+            else fill_entry(ty, e - jm, km, dy_loc, y, ny);
+        }
         __syncwarp();
         // pixels the cell can reach (the edges are nondecreasing)
         const int Plo = max(tx.edge[0], 0), Phi = min(tx.edge[jm], nx - 1);
@@ -280,42 +296,50 @@ __global__ void __launch_bounds__(OA_BLOCK) offaxis_kernel(const ytgb_offaxis_ar
         const int wp = wy < 32 ? wy : 32;
         const int groups = 32 / wp;
         const int g = lane / wp;
-        if (g >= groups) continue;
         const int j0 = g * jm / groups, j1 = (g + 1) * jm / groups;
         Column col;
         col.stamp = a.stamp + (long long)depth * a.nsx * a.nsy;
         col.nsy = a.nsy;
+        col.kcap = km - 1;
         col.nx = nx;
         col.npix = npix;
         col.cq = cq;
         col.cw = cw;
         col.buf = a.buffer;
         col.bufw = a.buffer_weight;
-        for (int qb = Qlo; qb <= Qhi; qb += wp) {
-            const int Q = qb + lane - g * wp;
-            if (Q > Qhi) continue;
-            const int klo = first_reaching(ty, km, Q), khi = last_starting(ty, km, Q);
-            const int nk = khi - klo + 1;
+        const int passes = (wy + wp - 1) / wp;
+        for (int pass = 0; pass < passes; pass++) {
+            const int Q = Qlo + pass * wp + lane - g * wp;
+            const bool act = g < groups && Q <= Qhi;
+            int klo = 0, nk = 0;
+            if (act) {
+                klo = first_reaching(ty, km, Q);
+                nk = last_starting(ty, km, Q) - klo + 1;
+            }
             col.klo = klo;
             col.Q = Q;
-            if (nk < 1) continue;
-            if (nk > OA_MAXK) {
-                column_rows_wide(tx, ty, col, khi, j0, j1);
+            // one unrolled length for the whole warp: lanes of different
+            // lengths would otherwise run their loops one after another
+            const int N = __reduce_max_sync(0xffffffffu, nk > 0 ? nk : 0);
+            if (!act || nk < 1) continue;
+            if (N > OA_MAXK) {
+                column_rows_wide(tx, ty, col, klo + nk - 1, j0, j1);
                 continue;
             }
-            // fy_k(Q) of the subcells meeting Q (image_utilities.pyx:141-159)
+            // fy_k(Q) of the subcells meeting Q (image_utilities.pyx:141-159),
+            // 0 past this lane's own nk
             double w[OA_MAXK];
 #pragma unroll
             for (int u = 0; u < OA_MAXK; u++) {
                 const int k = klo + u;
-                double v = 0.0;
+                double wv = 0.0;
                 if (u < nk) {
-                    if (ty.edge[k] == Q) v = ty.dv[k];
-                    if (ty.edge[k + 1] == Q) v = ytgb::dadd(v, ty.uv[k]);
+                    if (ty.edge[k] == Q) wv = ty.dv[k];
+                    if (ty.edge[k + 1] == Q) wv = ytgb::dadd(wv, ty.uv[k]);
                 }
-                w[u] = v;
+                w[u] = wv;
             }
-            switch (nk) {
+            switch (N) {
             case 1: column_rows<1>(tx, col, w, j0, j1); break;
             case 2: column_rows<2>(tx, col, w, j0, j1); break;
             case 3: column_rows<3>(tx, col, w, j0, j1); break;
