@@ -263,6 +263,21 @@ int ytgb_pack_fields(const double *const *src, const int64_t *count, const int64
  * values) to dst_lo: the low parts the light-source sampler's gradient uses. */
 int ytgb_pack_fields_split(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
                            float *dst_hi, float *dst_lo, int32_t n_threads);
+/* The same gather done by the device, for GPUs that read pageable host
+ * memory coherently (cudaDevAttrPageableMemoryAccess, e.g. a Grace CPU
+ * joined to its GPU by NVLink-C2C): the kernel reads the host float64 arrays
+ * src[k] directly and writes d_arena[dst_offset[k] + i] = (float)src[k][i]
+ * for i < count[k], and the low parts into d_arena_lo when it is not NULL
+ * (as ytgb_pack_fields_split).  src, count and dst_offset are host arrays,
+ * read by the device too; they and the fields must stay unchanged until the
+ * stream has passed the launch.  Every destination range is checked against
+ * arena_len on the host first.  Returns YTGB_ERR_INVALID, launching
+ * nothing, on a device without pageable memory access. */
+int ytgb_gather_fields(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
+                       float *d_arena, float *d_arena_lo, int64_t arena_len, void *stream);
+/* *out = 1 when the current device reads pageable host memory coherently
+ * (the condition of ytgb_gather_fields), else 0. */
+int ytgb_device_reads_host(int32_t *out);
 /* The same gather for uint8 cell masks (dst may be NULL: check only);
  * *all_ones = 1 when every mask byte is 1 (VolumeRenderSampler then needs no
  * mask, image_samplers.pyx:461-462). */

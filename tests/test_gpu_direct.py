@@ -1,0 +1,128 @@
+"""Bricks gathered by the device from the caller's host arrays
+(ytgb_gather_fields, on GPUs that read pageable host memory) against the
+host pack into pinned memory: the same float32 arena and low parts bit for
+bit, and the same drop-in sampler images."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from yt_gb300 import workloads
+from yt_gb300.volume import BrickSet, device_reads_host
+
+pytestmark = pytest.mark.gpu
+
+
+def fields(bs, lo=False):
+    """Each brick field's values in the arena (without the padding)."""
+    arena = (bs.data_lo if lo else bs.data).cpu().numpy()
+    d = bs.desc_host
+    out = []
+    for k in range(bs.n):
+        for f in range(int(d["n_fields"][k])):
+            o = int(d["data_offset"][k] + f * d["field_stride"][k])
+            out.append(arena[o: o + int(bs.verts[k])])
+    return np.concatenate(out)
+
+
+def odd_bricks(seed=4):
+    """Bricks with 1-3 fields of vertex data: views and transposes (not
+    C-contiguous), float32 input, NaN, infinities and values beyond float32."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(40):
+        dims = rng.integers(2, 9, 3)
+        shape = tuple(int(v) + 1 for v in dims)
+        data = []
+        for f in range(int(rng.integers(1, 4))):
+            a = rng.normal(0, 1, shape) * 10.0 ** rng.integers(-3, 4)
+            if k % 5 == 1:
+                a = np.ascontiguousarray(a.transpose(2, 1, 0)).transpose(2, 1, 0)  # F-order view
+            if k % 7 == 2:
+                a = a.astype(np.float32)
+            if k % 6 == 3:
+                flat = a.reshape(-1)
+                flat[:4] = [np.nan, np.inf, -np.inf, 1e300]
+            data.append(a)
+        le = rng.uniform(0, 0.5, 3)
+        out.append((data, np.ones(tuple(int(v) for v in dims), np.uint8), le, le + 0.5, dims))
+    return out
+
+
+@pytest.mark.parametrize("with_lo", [False, True])
+def test_direct_gather_matches_host_pack(cuda, with_lo):
+    if not device_reads_host(cuda):
+        pytest.skip("the device does not read pageable host memory")
+    bricks = odd_bricks()
+    a = BrickSet(bricks, device=cuda, with_lo=with_lo, direct=False)
+    b = BrickSet(bricks, device=cuda, with_lo=with_lo, direct=True)
+    assert b.direct and not a.direct
+    assert np.array_equal(a.desc.cpu().numpy(), b.desc.cpu().numpy())
+    for lo in ((False, True) if with_lo else (False,)):
+        x, y = fields(a, lo), fields(b, lo)
+        # NaN payloads differ between host and device conversions
+        nan = np.isnan(x)
+        assert np.array_equal(nan, np.isnan(y)) and (lo or nan.any())
+        assert np.array_equal(x[~nan].view(np.int32), y[~nan].view(np.int32))
+
+
+def test_direct_sampler_matches_host_pack(cuda):
+    """The drop-in VolumeRenderSampler with device gather and direct
+    download against the host pack and staged download: identical images."""
+    if not device_reads_host(cuda):
+        pytest.skip("the device does not read pageable host memory")
+    from yt_gb300.image_samplers import VolumeRenderSampler
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=64)
+    cam = w.views[0].camera
+    imgs = []
+    for host_pack in ("1", "0"):
+        os.environ["YTGB_HOST_PACK"] = host_pack
+        try:
+            p = cam.sampler_params()
+            s = VolumeRenderSampler(np.atleast_3d(p["vp_pos"]), np.atleast_3d(p["vp_dir"]), p["center"],
+                                    p["bounds"], p["image"], p["x_vec"], p["y_vec"], p["width"], "KDTree", w.tf, 1,
+                                    lens_type=p["lens_type"], camera_data=p["camera_data"])
+            for pg in w.kdtree.traverse(cam.viewpoint):
+                s(pg, num_threads=0)
+            imgs.append(s.aimage.copy())
+        finally:
+            os.environ.pop("YTGB_HOST_PACK", None)
+    assert np.abs(imgs[0]).max() > 0
+    assert np.array_equal(imgs[0].view(np.int64), imgs[1].view(np.int64))
+
+
+@pytest.mark.parametrize("case", ["image", "zbuffer", "both"])
+def test_sampler_rerenders_when_inputs_are_not_default(cuda, case):
+    """The drop-in sampler launches at once on a zero image and no zbuffer
+    and checks the caller's arrays meanwhile: an image that already holds
+    values (accumulation) or a zbuffer below 1 makes it render again on the
+    real inputs, matching the oracle's image and sample count."""
+    from test_gpu_parity import oracle_render
+    from yt_gb300 import _lib
+    from yt_gb300.image_samplers import VolumeRenderSampler
+    from yt_gb300.render import relative_error
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=48)
+    cam = w.views[0].camera
+    p = cam.sampler_params()
+    rng = np.random.default_rng(9)
+    nx, ny = p["image"].shape[:2]
+    init = np.zeros((nx, ny, 4))
+    if case in ("image", "both"):
+        init = rng.uniform(0.0, 0.5, (nx, ny, 4))
+    zb = np.ones((nx, ny))
+    if case in ("zbuffer", "both"):
+        zb = rng.uniform(0.2, 1.0, (nx, ny))
+    img = init.copy()
+    s = VolumeRenderSampler(np.atleast_3d(p["vp_pos"]), np.atleast_3d(p["vp_dir"]), p["center"], p["bounds"], img,
+                            p["x_vec"], p["y_vec"], p["width"], "KDTree", w.tf, 1, lens_type=p["lens_type"],
+                            camera_data=p["camera_data"], zbuffer=zb)
+    for pg in w.kdtree.traverse(cam.viewpoint):
+        s(pg, num_threads=0)
+    out = s.aimage
+    ref, visits, _, _ = oracle_render(w.bricks, cam, w.order(cam), _lib.VOLUME_RENDER, tf=w.tf,
+                                      zbuffer=None if case == "image" else zb, image=init)
+    assert relative_error(out, ref, channels=(0, 1, 2))[0] <= 1e-5
+    assert int(s.last_counters[0]) == visits

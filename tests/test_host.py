@@ -264,3 +264,42 @@ def test_leaf_slices_match_brick():
         v = kd._vertex(g)
         s = v[li[k][0]: li[k][0] + d[0] + 1, li[k][1]: li[k][1] + d[1] + 1, li[k][2]: li[k][2] + d[2] + 1]
         assert np.array_equal(s, data[0], equal_nan=True)
+
+
+def test_native_brick_scan_matches_python():
+    """_ytgb_marshal.scan flattens a sampler's bricks exactly as the Python
+    scan does, and declines bricks that need converting."""
+    from yt_gb300 import volume
+    from yt_gb300.partitioned_grid import PartitionedGrid
+    from yt_gb300.image_samplers import brick_tuple
+
+    if volume._marshal() is None:
+        pytest.skip("_ytgb_marshal not built")
+    rng = np.random.default_rng(3)
+    bricks = []
+    for k in range(30):
+        dims = rng.integers(1, 7, 3)
+        data = [rng.random(tuple(int(d) + 1 for d in dims)) for _ in range(int(rng.integers(1, 4)))]
+        mask = None if k % 4 == 0 else np.ones(tuple(int(d) for d in dims), np.uint8)
+        le = rng.random(3)
+        bricks.append((data, mask, le if k % 3 else list(le), le + 1.0, tuple(int(d) for d in dims)))
+    bricks.append(brick_tuple(PartitionedGrid(0, [rng.random((3, 4, 5))], np.ones((2, 3, 4), np.uint8),
+                                              np.zeros(3), np.ones(3), np.array([2, 3, 4]))))
+    n = len(bricks)
+
+    def arrays():
+        return np.ones((n, 3), np.int64), np.zeros((n, 3)), np.ones((n, 3)), np.zeros(n, np.int64)
+
+    a = arrays()
+    got = volume._scan(bricks, n, *a)
+    assert got is not None
+    b = arrays()
+    ref = volume.BrickSet.__new__(volume.BrickSet)._scan_python(bricks, n, *b)
+    for x, y in zip(got + a, ref + b):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
+    # a Fortran-ordered field, a float32 field or a bool mask: left to Python
+    for bad in ([np.asfortranarray(rng.random((3, 3, 3)))], [rng.random((3, 3, 3)).astype(np.float32)]):
+        odd = list(bricks) + [(bad, None, np.zeros(3), np.ones(3), (2, 2, 2))]
+        assert volume._scan(odd, len(odd), *[np.resize(v, (len(odd),) + v.shape[1:]) for v in arrays()]) is None
+    odd = list(bricks) + [([rng.random((3, 3, 3))], np.ones((2, 2, 2), bool), np.zeros(3), np.ones(3), (2, 2, 2))]
+    assert volume._scan(odd, len(odd), *[np.resize(v, (len(odd),) + v.shape[1:]) for v in arrays()]) is None

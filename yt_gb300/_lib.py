@@ -196,6 +196,9 @@ SIGNATURES = {
     "ytgb_octree_destroy": (None, [C.c_void_p]),
     "ytgb_render_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_offaxis_cells": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_gather_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                     C.c_int64, C.c_void_p]),
+    "ytgb_device_reads_host": (C.c_int, [C.c_void_p]),
     "ytgb_trace_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
     "ytgb_pack_masks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,

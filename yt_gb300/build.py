@@ -13,6 +13,7 @@ import os
 import shutil
 import subprocess
 import sys
+import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
@@ -26,6 +27,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ytgb_render.cu", "ytgb_prep.cu", "ytgb_octree.cu", "ytgb_offaxis.cu"]
 CPP_SOURCES = ["ytgb_host.cpp", "ytgb_pack.cpp"]
+# the CPython extension that scans a sampler's bricks natively
+MARSHAL_SOURCE = CSRC / "ytgb_pymarshal.cpp"
+MARSHAL = OUTDIR / ("_ytgb_marshal" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
 
 
 def _nvcc() -> str:
@@ -41,10 +45,27 @@ def _sources():
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not MARSHAL.exists() or MARSHAL.stat().st_mtime < MARSHAL_SOURCE.stat().st_mtime:
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _sources() if p.exists())
+
+
+def build_marshal() -> Path:
+    """Compile the ``_ytgb_marshal`` CPython extension (plain C API, no
+    numpy headers) next to libytgb.so."""
+    OUTDIR.mkdir(parents=True, exist_ok=True)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("a C++ compiler is required to build _ytgb_marshal")
+    tmp = MARSHAL.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", f"-I{sysconfig.get_paths()['include']}",
+           str(MARSHAL_SOURCE), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, MARSHAL)
+    return MARSHAL
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -72,8 +93,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return obj
 
     srcs = [CSRC / s for s in CU_SOURCES + CPP_SOURCES]
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=min(8, len(srcs) + 1)) as ex:
+        marshal = ex.submit(build_marshal)
         objs = list(ex.map(compile_one, srcs))
+        marshal.result()
     tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -209,8 +209,14 @@ extern "C" int ytgb_host_prefault(void *p, int64_t bytes) {
     if (page <= 0 || bytes == 0) return YTGB_OK;
     const uintptr_t a = (uintptr_t)p, e = a + (uintptr_t)bytes;
     const uintptr_t lo = (a + page - 1) / page * page, hi = e / page * page;
-    // whole pages inside [p, p + bytes) only; failure (older kernel, an
-    // unusual mapping) just leaves the pages to fault on first write
-    if (hi > lo) (void)madvise((void *)lo, hi - lo, MADV_POPULATE_WRITE);
+    if (hi <= lo) return YTGB_OK;
+    // whole pages inside [p, p + bytes) only, split over host threads (the
+    // kernel zero-fills each new page: one thread populated a 32 MiB image
+    // in ~1 ms on the Grace host); failure (older kernel, an unusual
+    // mapping) just leaves the pages to fault on first write
+    const int64_t pages = (int64_t)((hi - lo) / page);
+    parallel_ranges(pages, thread_count(0, (int64_t)(hi - lo)), [&](int64_t p0, int64_t p1) {
+        if (p1 > p0) (void)madvise((void *)(lo + p0 * page), (size_t)((p1 - p0) * page), MADV_POPULATE_WRITE);
+    });
     return YTGB_OK;
 }

@@ -69,7 +69,81 @@ vertex_bricks_kernel(const double *cells, int64_t n_cells, const int64_t *grid_o
     }
 }
 
+constexpr int GATHER_BLOCK = 256;
+
+// One block per field (grid-stride over the fields): host float64 values,
+// read over the CPU-GPU link, to float32 (and low parts) in the arena.
+__global__ void __launch_bounds__(GATHER_BLOCK)
+gather_fields_kernel(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
+                     float *arena, float *arena_lo) {
+    for (int64_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const double *s = src[k];
+        const int64_t c = count[k];
+        float *d = arena + dst_offset[k];
+        float *dl = arena_lo ? arena_lo + dst_offset[k] : nullptr;
+        for (int64_t i = threadIdx.x; i < c; i += GATHER_BLOCK) {
+            const double v = s[i];
+            const float h = (float)v;
+            d[i] = h;
+            if (dl) {
+                const double r = v - (double)h;
+                dl[i] = r == r && r - r == 0.0 ? (float)r : 0.0f;
+            }
+        }
+    }
+}
+
+bool device_reads_host() {
+    int dev = 0, pma = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+    return pma != 0;
+}
+
 }  // namespace
+
+extern "C" int ytgb_device_reads_host(int32_t *out) {
+    if (!out) {
+        ytgb_set_error("ytgb_device_reads_host: null out");
+        return YTGB_ERR_INVALID;
+    }
+    *out = device_reads_host() ? 1 : 0;
+    return YTGB_OK;
+}
+
+extern "C" int ytgb_gather_fields(const double *const *src, const int64_t *count, const int64_t *dst_offset,
+                                  int64_t n, float *d_arena, float *d_arena_lo, int64_t arena_len, void *stream) {
+    if (n < 0 || arena_len < 0 || (n > 0 && (!src || !count || !dst_offset || !d_arena))) {
+        ytgb_set_error("ytgb_gather_fields: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    if (n == 0) return YTGB_OK;
+    if (!device_reads_host()) {
+        ytgb_set_error("ytgb_gather_fields: the device cannot read pageable host memory");
+        return YTGB_ERR_INVALID;
+    }
+    if (((uintptr_t)d_arena & 3) || ((uintptr_t)d_arena_lo & 3)) {
+        ytgb_set_error("ytgb_gather_fields: misaligned arena");
+        return YTGB_ERR_INVALID;
+    }
+    for (int64_t k = 0; k < n; k++) {
+        if (count[k] < 0 || (count[k] > 0 && (!src[k] || ((uintptr_t)src[k] & 7))) || dst_offset[k] < 0 ||
+            dst_offset[k] > arena_len - count[k]) {
+            ytgb_set_error("ytgb_gather_fields: field " + std::to_string(k) + " is null, misaligned or does not "
+                           "fit the arena");
+            return YTGB_ERR_INVALID;
+        }
+    }
+    const int blocks = (int)(n < 152 * 16 ? n : 152 * 16);
+    gather_fields_kernel<<<blocks, GATHER_BLOCK, 0, (cudaStream_t)stream>>>(src, count, dst_offset, n, d_arena,
+                                                                           d_arena_lo);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_gather_fields: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    return YTGB_OK;
+}
 
 extern "C" int ytgb_vertex_bricks(const double *d_cells, int64_t n_cells, const int64_t *d_grid_offset,
                                   const int32_t *d_grid_dims, int32_t n_grids, const int32_t *d_brick_grid,

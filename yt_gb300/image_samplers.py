@@ -226,56 +226,84 @@ class ImageSampler:
         dev = _device()
         L = _lib.lib()
         t0 = time.perf_counter()
-        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev, with_lo=self._with_lo)
-        order = np.arange(len(pending), dtype=np.int32)
-        nx, ny = self.nv
-        t1 = time.perf_counter()
-        # The caller's image, updated in place.  An image of zero bits (a new
-        # image) is cleared on the device instead of copied; a zbuffer of
-        # ones clips nothing (image_samplers.pyx:185, max_t = 1) and is left
-        # out.  Both checks read the host arrays once on all cores.
         img = self._image
         if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
             img = np.ascontiguousarray(img, dtype=np.float64)
-        flag = C.c_int32()
-        # the result is written into img below: fault its pages in for
-        # writing first, so that reading it here does not map the shared
-        # zero page (and make every page a copy-on-write fault later)
-        _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
-        _lib.check(L.ytgb_host_is_uniform(img.ctypes.data, img.size, 0.0, 0, C.byref(flag)), "image check")
-        h2d = 0
-        if flag.value:
-            image_d = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev)
-        else:
-            image_d = torch.from_numpy(img).to(dev)
-            h2d += img.nbytes
         zb = np.ascontiguousarray(self.azbuffer, dtype=np.float64)
-        _lib.check(L.ytgb_host_is_uniform(zb.ctypes.data, zb.size, 1.0, 0, C.byref(flag)), "zbuffer check")
-        zb_d = None
-        if not flag.value:
-            zb_d = torch.from_numpy(zb).to(dev)
-            h2d += zb.nbytes
+        # The render is launched on the usual inputs -- a new image (all zero
+        # bits) and a zbuffer of ones, which clips nothing
+        # (image_samplers.pyx:185, max_t = 1) -- while a host thread checks
+        # that they are: it faults the image's pages in for writing (so that
+        # its read does not map the shared zero page and make every page a
+        # copy-on-write fault later) and reads both arrays on all cores.
+        # Other inputs are uploaded and the view rendered again.
+        checks = {}
+
+        def host_checks():
+            try:
+                flag = C.c_int32()
+                _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
+                _lib.check(L.ytgb_host_is_uniform(img.ctypes.data, img.size, 0.0, 0, C.byref(flag)), "image check")
+                checks["img_zero"] = bool(flag.value)
+                _lib.check(L.ytgb_host_is_uniform(zb.ctypes.data, zb.size, 1.0, 0, C.byref(flag)),
+                           "zbuffer check")
+                checks["zb_ones"] = bool(flag.value)
+            except BaseException as e:  # re-raised on the calling thread
+                checks["error"] = e
+
+        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev, with_lo=self._with_lo)
+        t1 = time.perf_counter()
+        checker = threading.Thread(target=host_checks, daemon=True)
+        checker.start()
+        order = np.arange(len(pending), dtype=np.int32)
+        nx, ny = self.nv
         px_pos = px_dir = None
+        h2d = 0
         if self._px_pos is not None:
             px_pos = torch.from_numpy(self._px_pos).to(dev)
             px_dir = torch.from_numpy(self._px_dir).to(dev)
             h2d += self._px_pos.nbytes + self._px_dir.nbytes
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)
-        torch.cuda.synchronize(dev)
-        t2 = time.perf_counter()
-        _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb_d,
-                n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
-                px_pos=px_pos, px_dir=px_dir, light=self._light())
         stream = torch.cuda.current_stream(dev)
+        keep = []
+
+        def launch(image_d, zb_d):
+            _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb_d,
+                    n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
+                    px_pos=px_pos, px_dir=px_dir, light=self._light(), keep=keep)
+
+        image_d = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev)
+        try:
+            launch(image_d, None)
+        finally:
+            checker.join()
+        if "error" in checks:
+            raise checks["error"]
+        img_zero, zb_ones = checks["img_zero"], checks["zb_ones"]
+        if not (img_zero and zb_ones):
+            image_d = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev) if img_zero else \
+                torch.from_numpy(img).to(dev)
+            zb_d = None if zb_ones else torch.from_numpy(zb).to(dev)
+            h2d += (0 if img_zero else img.nbytes) + (0 if zb_ones else zb.nbytes)
+            counters.zero_()
+            error.zero_()
+            launch(image_d, zb_d)
+        t2 = time.perf_counter()
         _lib.check(L.ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
+        keep.clear()
         t3 = time.perf_counter()
-        # device -> pinned staging (full link speed), then into the caller's
-        # array on all host cores
-        with _stage["lock"]:
-            stage = _staging(img.nbytes)[: img.size].view(image_d.shape)
-            stage.copy_(image_d)
-            _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
+        if bricks.direct:
+            # a device that reads and writes pageable host memory copies
+            # straight into the caller's (prefaulted) array at link speed
+            torch.from_numpy(img).copy_(image_d)
+        else:
+            # device -> pinned staging (full link speed), then into the
+            # caller's array on all host cores
+            with _stage["lock"]:
+                stage = _staging(img.nbytes)[: img.size].view(image_d.shape)
+                stage.copy_(image_d)
+                _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
         if img is not self._image:
             self._image[...] = img
         self.last_counters = counters.cpu().numpy()
@@ -285,7 +313,10 @@ class ImageSampler:
         # per-pixel rays were needed) and device -> host (image, counters)
         self.last_h2d_bytes = int(bricks.upload_bytes + h2d + 20 * len(pending))
         self.last_d2h_bytes = int(img.nbytes + 4 * 8)
-        self.last_timings = {"pack_ms": 1e3 * (t1 - t0), "upload_ms": 1e3 * (t2 - t1), "render_ms": 1e3 * (t3 - t2),
+        # pack: bricks into the arena; launch: launch, host checks (the
+        # device renders meanwhile); render: the rest of the render;
+        # download: the image into the caller's array
+        self.last_timings = {"pack_ms": 1e3 * (t1 - t0), "launch_ms": 1e3 * (t2 - t1), "render_ms": 1e3 * (t3 - t2),
                              "download_ms": 1e3 * (t4 - t3)}
 
     def ensure_code_unit_params(self, params):

@@ -26,6 +26,73 @@ def _pinned(shape, dtype, device) -> torch.Tensor:
     return torch.empty(shape, dtype=dtype, pin_memory=torch.device(device).type == "cuda")
 
 
+_MARSHAL: list = []
+
+
+def _marshal():
+    """The native brick scanner (``_ytgb_marshal``, built with libytgb), or
+    None where it is not built: the Python scan then does the same work."""
+    if not _MARSHAL:
+        mod = None
+        try:
+            import importlib.util
+
+            from .build import MARSHAL
+
+            if MARSHAL.exists():
+                spec = importlib.util.spec_from_file_location("_ytgb_marshal", MARSHAL)
+                mod = importlib.util.module_from_spec(spec)
+                spec.loader.exec_module(mod)
+        except ImportError:
+            mod = None
+        _MARSHAL.append(mod)
+    return _MARSHAL[0]
+
+
+def _scan(bricks, n, dims, le, re, nfields):
+    """Brick scan by ``_ytgb_marshal.scan``: (field addresses, field sizes,
+    masked bricks, their mask addresses, their mask sizes), filling dims, le,
+    re and nfields; None when the module is missing or a brick needs
+    converting (the Python scan handles those)."""
+    mod = _marshal()
+    if mod is None or n == 0:
+        return None
+    cap = 6 * n
+    fptr = np.empty(cap, dtype=np.uintp)
+    fsize = np.empty(cap, dtype=np.int64)
+    mptr = np.empty(n, dtype=np.uintp)
+    msz = np.empty(n, dtype=np.int64)
+    got = mod.scan(bricks, cap, fptr.ctypes.data, fsize.ctypes.data, nfields.ctypes.data, dims.ctypes.data,
+                   le.ctypes.data, re.ctypes.data, mptr.ctypes.data, msz.ctypes.data)
+    if got is False:
+        return None
+    mk = np.nonzero(msz >= 0)[0]
+    return fptr[:got], fsize[:got], mk, mptr[mk], msz[mk]
+
+
+_READS_HOST: dict = {}
+
+
+def device_reads_host(device) -> bool:
+    """Whether ``device`` reads pageable host memory coherently (a Grace CPU
+    and its GPU joined by NVLink-C2C): bricks are then gathered from the
+    caller's host arrays by the device (``ytgb_gather_fields``) instead of
+    packed on the host and copied.  ``YTGB_HOST_PACK=1`` forces the host
+    pack."""
+    import os
+
+    dev = torch.device(device)
+    if dev.type != "cuda" or os.environ.get("YTGB_HOST_PACK") == "1":
+        return False
+    idx = dev.index if dev.index is not None else torch.cuda.current_device()
+    if idx not in _READS_HOST:
+        out = C.c_int32()
+        with torch.cuda.device(idx):
+            _lib.check(_lib.lib().ytgb_device_reads_host(C.byref(out)), "ytgb_device_reads_host")
+        _READS_HOST[idx] = bool(out.value)
+    return _READS_HOST[idx]
+
+
 def _address(a: np.ndarray) -> int:
     """Data address of a C-contiguous array (through the buffer protocol,
     which is cheaper than ``a.ctypes.data``; read-only arrays take the slow
@@ -55,11 +122,95 @@ class BrickSet:
     samplers index them exactly as yt does), ``mask`` a uint8 array of
     ``dims`` or None (all ones)."""
 
-    def __init__(self, bricks: Sequence, device="cuda", with_lo=False):
+    def __init__(self, bricks: Sequence, device="cuda", with_lo=False, direct=None):
         self.device = torch.device(device)
+        direct = device_reads_host(self.device) if direct is None else bool(direct)
+        self.direct = direct
         n = len(bricks)
         self.n = n
         m = max(n, 1)
+        dims = np.ones((m, 3), dtype=np.int64)
+        le = np.zeros((m, 3))
+        re = np.ones((m, 3))
+        nfields = np.zeros(m, dtype=np.int64)
+        scanned = _scan(bricks, n, dims, le, re, nfields)
+        if scanned is not None:
+            src, fsize, mk_brick, mptr, mk_size = scanned
+        else:
+            src, fsize, mk_brick, mptr, mk_size = self._scan_python(bricks, n, dims, le, re, nfields)
+        bad = np.nonzero((dims[:n] <= 0).any(axis=1) | (nfields[:n] < 1) | (nfields[:n] > 6))[0]
+        if bad.size:
+            k = int(bad[0])
+            raise ValueError(f"brick {k}: dims must be 3 positive integers and 1 to 6 fields are supported "
+                             f"(dims {dims[k].tolist()}, {int(nfields[k])} fields)")
+        if mk_brick.size:
+            wrong = np.nonzero(mk_size != dims[mk_brick].prod(axis=1))[0]
+            if wrong.size:
+                raise ValueError(f"brick {int(mk_brick[wrong[0]])}: mask must have prod(dims) entries")
+        fstart = np.concatenate([[0], np.cumsum(nfields[:n])]).astype(np.int64)
+        sizes_min = np.minimum.reduceat(fsize, fstart[:-1]) if n else fsize
+        sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
+        desc, stride, data_off, total, bounds = self._layout(dims, le, re, nfields, sizes_min, sizes_max)
+        L = _lib.lib()
+        fbrick = np.repeat(np.arange(n), nfields[:n])
+        dst_f = (data_off[fbrick] + (np.arange(len(src)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
+        arena_len = max(total, 4)
+        if direct:
+            # the device reads the caller's float64 arrays over the CPU-GPU
+            # link and writes the float32 arena itself
+            buf = torch.empty((arena_len,), dtype=torch.float32, device=self.device)
+            buf_lo = torch.empty((arena_len,), dtype=torch.float32, device=self.device) if with_lo else None
+            stream = torch.cuda.current_stream(self.device)
+            _lib.check(L.ytgb_gather_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
+                                            buf.data_ptr(), buf_lo.data_ptr() if buf_lo is not None else None,
+                                            arena_len, C.c_void_p(stream.cuda_stream)), "ytgb_gather_fields")
+        else:
+            # float64 -> float32 gather into the pinned arena, on all host cores
+            buf = _pinned((arena_len,), torch.float32, self.device)
+            buf_lo = _pinned((arena_len,), torch.float32, self.device) if with_lo else None
+            if with_lo:
+                _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data,
+                                                    len(src), buf.data_ptr(), buf_lo.data_ptr(), 0),
+                           "ytgb_pack_fields_split")
+            else:
+                _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
+                                              buf.data_ptr(), 0), "ytgb_pack_fields")
+        # masks: kept only when some cell is masked out
+        mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
+        desc["mask_offset"][:] = -1
+        mbuf = None
+        if mk_brick.size:
+            msrc = np.ascontiguousarray(mptr, dtype=np.uintp)
+            mcnt = np.ascontiguousarray(mk_size, dtype=np.int64)
+            mdst = np.ascontiguousarray(mstart[mk_brick])
+            ones = C.c_int32()
+            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, mk_brick.size, None,
+                                         0, C.byref(ones)), "ytgb_pack_masks")
+            if not ones.value:
+                mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
+                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, mk_brick.size,
+                                             mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
+                desc["mask_offset"][mk_brick] = mdst
+        self.desc_host = desc
+        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
+        self.data = buf.to(self.device, non_blocking=True)
+        self.data_lo = buf_lo.to(self.device, non_blocking=True) if buf_lo is not None else None
+        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
+        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
+        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
+        if direct:
+            # the caller's arrays (and the converted copies in keep) may
+            # change or go once this returns: let the device finish reading
+            torch.cuda.current_stream(self.device).synchronize()
+        self.nbytes = int(self.data.numel() * 4)
+        self.upload_bytes = int(self.data.numel() * 4 * (2 if with_lo else 1) + self.bounds.numel() * 8 +
+                                self.desc.numel() + (self.masks.numel() if self.masks is not None else 0))
+
+    def _scan_python(self, bricks, n, dims, le, re, nfields):
+        """The brick scan in Python (any array types): field addresses and
+        sizes, masked bricks with their mask addresses and sizes; fills dims,
+        le, re and nfields.  Converted arrays are kept on the instance until
+        the arena has been written."""
         f64 = np.dtype(np.float64)
         u8 = np.dtype(np.uint8)
         dims_l, le_l, re_l, nf_l = [], [], [], []
@@ -87,10 +238,6 @@ class BrickSet:
                 mk_k.append(k)
                 mptr.append(addr(mk))
                 msz.append(mk.size)
-        dims = np.ones((m, 3), dtype=np.int64)
-        le = np.zeros((m, 3))
-        re = np.ones((m, 3))
-        nfields = np.zeros(m, dtype=np.int64)
         if n:
             try:
                 dims[:n] = np.array(dims_l, dtype=np.int64).reshape(n, 3)
@@ -99,61 +246,9 @@ class BrickSet:
             le[:n] = np.array(le_l, dtype=np.float64).reshape(n, -1)[:, :3]
             re[:n] = np.array(re_l, dtype=np.float64).reshape(n, -1)[:, :3]
             nfields[:n] = nf_l
-        bad = np.nonzero((dims[:n] <= 0).any(axis=1) | (nfields[:n] < 1) | (nfields[:n] > 6))[0]
-        if bad.size:
-            k = int(bad[0])
-            raise ValueError(f"brick {k}: dims must be 3 positive integers and 1 to 6 fields are supported "
-                             f"(dims {dims[k].tolist()}, {int(nfields[k])} fields)")
-        if mk_k:
-            mk_brick = np.array(mk_k, dtype=np.int64)
-            mk_size = np.array(msz, dtype=np.int64)
-            wrong = np.nonzero(mk_size != dims[mk_brick].prod(axis=1))[0]
-            if wrong.size:
-                raise ValueError(f"brick {int(mk_brick[wrong[0]])}: mask must have prod(dims) entries")
-        fsize = np.array(fsz, dtype=np.int64)
-        fstart = np.concatenate([[0], np.cumsum(nfields[:n])]).astype(np.int64)
-        sizes_min = np.minimum.reduceat(fsize, fstart[:-1]) if n else fsize
-        sizes_max = np.maximum.reduceat(fsize, fstart[:-1]) if n else fsize
-        desc, stride, data_off, total, bounds = self._layout(dims, le, re, nfields, sizes_min, sizes_max)
-        buf = _pinned((max(total, 4),), torch.float32, self.device)
-        buf_lo = _pinned((max(total, 4),), torch.float32, self.device) if with_lo else None
-        L = _lib.lib()
-        # float64 -> float32 gather into the pinned arena, on all host cores
-        src = np.array(fptr, dtype=np.uintp)
-        fbrick = np.repeat(np.arange(n), nfields[:n])
-        dst_f = (data_off[fbrick] + (np.arange(len(fptr)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
-        if with_lo:
-            _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
-                                                buf.data_ptr(), buf_lo.data_ptr(), 0), "ytgb_pack_fields_split")
-        else:
-            _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(fptr),
-                                          buf.data_ptr(), 0), "ytgb_pack_fields")
-        # masks: kept only when some cell is masked out
-        mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
-        desc["mask_offset"][:] = -1
-        mbuf = None
-        if mk_k:
-            msrc = np.array(mptr, dtype=np.uintp)
-            mcnt = mk_size
-            mdst = mstart[mk_brick]
-            ones = C.c_int32()
-            _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k), None, 0,
-                                         C.byref(ones)), "ytgb_pack_masks")
-            if not ones.value:
-                mbuf = _pinned((max(int(mstart[-1]), 1),), torch.uint8, self.device)
-                _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, len(mk_k),
-                                             mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
-                desc["mask_offset"][mk_brick] = mdst
-        self.desc_host = desc
-        self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
-        self.data = buf.to(self.device, non_blocking=True)
-        self.data_lo = buf_lo.to(self.device, non_blocking=True) if buf_lo is not None else None
-        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
-        self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
-        self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
-        self.nbytes = int(self.data.numel() * 4)
-        self.upload_bytes = int(self.data.numel() * 4 * (2 if with_lo else 1) + self.bounds.numel() * 8 +
-                                self.desc.numel() + (self.masks.numel() if self.masks is not None else 0))
+        self._keep = keep
+        return (np.array(fptr, dtype=np.uintp), np.array(fsz, dtype=np.int64), np.array(mk_k, dtype=np.int64),
+                np.array(mptr, dtype=np.uintp), np.array(msz, dtype=np.int64))
 
     @classmethod
     def on_device(cls, dims, le, re, device="cuda", n_fields=1, with_lo=False):
