@@ -77,6 +77,17 @@ typedef struct ytgb_brick {
     int32_t pad[5];
 } ytgb_brick;
 
+/* The device layout of n bricks: their descriptors (the VolumeContainer
+ * fields of PartitionedGrid.__cinit__, partitioned_grid.pyx:47-63, in the
+ * same float64 operations, plus arena offsets: each field sizes_max[k]
+ * floats rounded up to a multiple of 4, the bricks' fields back to back;
+ * mask_offset -1) and the cell-boundary tables k*dds + le, k = 0..dims,
+ * per brick and axis, into bounds (sum of dims+1 entries).  *arena_len is
+ * the arena's length in floats. */
+int ytgb_brick_layout(int64_t n, const int64_t *dims, const double *le, const double *re, const int64_t *n_fields,
+                      const int64_t *sizes_max, ytgb_brick *desc, double *bounds, int64_t bounds_len,
+                      int64_t *arena_len);
+
 /* One view: the ray-generation and culling fields of ImageSampler
  * (image_samplers.pxd:38-70, set in ImageSampler.__init__ :59-131). */
 typedef struct ytgb_view {

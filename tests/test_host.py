@@ -283,8 +283,10 @@ def test_native_brick_scan_matches_python():
         mask = None if k % 4 == 0 else np.ones(tuple(int(d) for d in dims), np.uint8)
         le = rng.random(3)
         bricks.append((data, mask, le if k % 3 else list(le), le + 1.0, tuple(int(d) for d in dims)))
-    bricks.append(brick_tuple(PartitionedGrid(0, [rng.random((3, 4, 5))], np.ones((2, 3, 4), np.uint8),
-                                              np.zeros(3), np.ones(3), np.array([2, 3, 4]))))
+    pg = PartitionedGrid(0, [rng.random((3, 4, 5))], np.ones((2, 3, 4), np.uint8), np.zeros(3), np.ones(3),
+                         np.array([2, 3, 4]))
+    bricks.append(brick_tuple(pg))
+    bricks.append(pg)  # the object itself: its attributes are read
     n = len(bricks)
 
     def arrays():
@@ -303,3 +305,36 @@ def test_native_brick_scan_matches_python():
         assert volume._scan(odd, len(odd), *[np.resize(v, (len(odd),) + v.shape[1:]) for v in arrays()]) is None
     odd = list(bricks) + [([rng.random((3, 3, 3))], np.ones((2, 2, 2), bool), np.zeros(3), np.ones(3), (2, 2, 2))]
     assert volume._scan(odd, len(odd), *[np.resize(v, (len(odd),) + v.shape[1:]) for v in arrays()]) is None
+
+
+def test_native_brick_layout_matches_numpy():
+    """ytgb_brick_layout's descriptors and cell-boundary tables equal the
+    numpy elementwise formulas (PartitionedGrid.__cinit__'s dds = (RE-LE)/dims,
+    idds = 1/dds; the tables k*dds + le) bit for bit."""
+    from yt_gb300.volume import BrickSet
+
+    rng = np.random.default_rng(8)
+    n = 25
+    dims = rng.integers(1, 20, (n, 3)).astype(np.int64)
+    le = rng.uniform(-1, 1, (n, 3))
+    re = le + rng.uniform(1e-3, 2, (n, 3))
+    nfields = rng.integers(1, 4, n).astype(np.int64)
+    sizes = (dims + 1).prod(axis=1)
+    bs = BrickSet.__new__(BrickSet)
+    bs.n = n
+    desc, stride, data_off, total, bounds = bs._layout(dims, le, re, nfields, sizes, sizes)
+    dds = (re - le) / dims
+    assert np.array_equal(desc["dds"], dds) and np.array_equal(desc["idds"], 1.0 / dds)
+    assert np.array_equal(desc["snap"], 1e-10 * dds)
+    assert np.array_equal(desc["lef"], le.astype(np.float32)) and np.array_equal(desc["iddsf"],
+                                                                                  (1.0 / dds).astype(np.float32))
+    st = (sizes + 3) & ~3
+    assert np.array_equal(stride, st) and np.array_equal(data_off, np.concatenate([[0], np.cumsum(st * nfields)])[:n])
+    assert total == int((st * nfields).sum())
+    cnt = (dims + 1).ravel()
+    starts = np.concatenate([[0], np.cumsum(cnt)])
+    kk = np.arange(starts[-1], dtype=np.float64) - np.repeat(starts[:-1], cnt)
+    ref = kk * np.repeat(dds.ravel(), cnt) + np.repeat(le.ravel(), cnt)
+    assert np.array_equal(bounds, ref)
+    assert np.array_equal(desc["bounds_offset"], starts[:-1].reshape(n, 3)[:, 0])
+    assert (desc["mask_offset"] == -1).all()

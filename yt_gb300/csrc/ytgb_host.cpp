@@ -128,6 +128,57 @@ static void extent_perspective(const ytgb_view *im, const ytgb_brick *vc, int64_
     rv[3] = std::min(max_py, im->ny);
 }
 
+extern "C" int ytgb_brick_layout(int64_t n, const int64_t *dims, const double *le, const double *re,
+                                 const int64_t *n_fields, const int64_t *sizes_max, ytgb_brick *desc, double *bounds,
+                                 int64_t bounds_len, int64_t *arena_len) {
+    if (n < 0 || (n > 0 && (!dims || !le || !re || !n_fields || !sizes_max || !desc || !bounds || !arena_len))) {
+        ytgb_set_error("ytgb_brick_layout: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    int64_t off = 0, boff = 0;
+    for (int64_t k = 0; k < n; k++) {
+        ytgb_brick &b = desc[k];
+        std::memset(&b, 0, sizeof(b));
+        const int64_t stride = (sizes_max[k] + 3) & ~(int64_t)3;
+        if (sizes_max[k] < 0 || n_fields[k] < 1 || n_fields[k] > 6) {
+            ytgb_set_error("ytgb_brick_layout: brick " + std::to_string(k) + ": bad field sizes");
+            return YTGB_ERR_INVALID;
+        }
+        for (int i = 0; i < 3; i++) {
+            const int64_t d = dims[3 * k + i];
+            if (d < 1 || d > (1 << 30) || boff + d + 1 > bounds_len) {
+                ytgb_set_error("ytgb_brick_layout: brick " + std::to_string(k) + ": bad dims or short table");
+                return YTGB_ERR_INVALID;
+            }
+            // PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55), elementwise
+            const double l = le[3 * k + i], r = re[3 * k + i];
+            const double dds = (r - l) / (double)d;
+            const double idds = 1.0 / dds;
+            b.left_edge[i] = l;
+            b.right_edge[i] = r;
+            b.dds[i] = dds;
+            b.idds[i] = idds;
+            b.snap[i] = 1e-10 * dds;
+            b.dims[i] = (int32_t)d;
+            b.lef[i] = (float)l;
+            b.ref[i] = (float)r;
+            b.iddsf[i] = (float)idds;
+            // cell-boundary table k*dds + le, k = 0..dims (the float64 values
+            // walk_volume forms for tmax, grid_traversal.pyx:106-108)
+            if (i == 0) b.bounds_offset = boff;
+            for (int64_t q = 0; q <= d; q++) bounds[boff + q] = (double)q * dds + l;
+            boff += d + 1;
+        }
+        b.n_fields = (int32_t)n_fields[k];
+        b.data_offset = off;
+        b.field_stride = stride;
+        b.mask_offset = -1;
+        off += stride * n_fields[k];
+    }
+    *arena_len = off;
+    return YTGB_OK;
+}
+
 extern "C" int ytgb_brick_rects(const ytgb_view *view, const ytgb_brick *bricks, int32_t n_bricks,
                                 const int32_t *order, int32_t n_order, int32_t *rects) {
     if (!view || !bricks || !rects || n_order < 0) {

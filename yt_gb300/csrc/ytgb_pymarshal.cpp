@@ -7,7 +7,9 @@
 // address and length of each field, the mask, the edges and the dims; a
 // Python loop over ~1000 bricks spends a couple of milliseconds on attribute
 // and type checks alone.  scan() does the same checks through the buffer
-// protocol in C and writes flat arrays the caller allocated.  A brick that
+// protocol in C, on (data, mask, left_edge, right_edge, dims) tuples or on
+// the PartitionedGrid objects themselves, and writes flat arrays the caller
+// allocated.  A brick that
 // is not in the expected form (a field that is not a C-contiguous native
 // float64 buffer, a mask that is not C-contiguous uint8, edges or dims that
 // are not 3 numbers, more than 6 fields) makes scan() return False, and the
@@ -83,8 +85,44 @@ bool three_ints(PyObject *o, int64_t out[3]) {
     return ok;
 }
 
+// One brick as (data, mask, left_edge, right_edge, dims): a 5-tuple, or an
+// object with yt's PartitionedGrid attributes my_data, source_mask,
+// LeftEdge and RightEdge (dims from the mask's shape).  New references in
+// out[0..4]; false when the object is neither.
+bool brick_parts(PyObject *t, PyObject *out[5]) {
+    if (PyTuple_Check(t)) {
+        if (PyTuple_GET_SIZE(t) != 5) return false;
+        for (int i = 0; i < 5; i++) {
+            out[i] = PyTuple_GET_ITEM(t, i);
+            Py_INCREF(out[i]);
+        }
+        return true;
+    }
+    static PyObject *names[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (!names[0]) {
+        const char *s[5] = {"my_data", "source_mask", "LeftEdge", "RightEdge", "shape"};
+        for (int i = 0; i < 5; i++) names[i] = PyUnicode_InternFromString(s[i]);
+    }
+    for (int i = 0; i < 4; i++) {
+        out[i] = PyObject_GetAttr(t, names[i]);
+        if (!out[i]) {
+            PyErr_Clear();
+            for (int j = 0; j < i; j++) Py_DECREF(out[j]);
+            return false;
+        }
+    }
+    out[4] = PyObject_GetAttr(out[1], names[4]);
+    if (!out[4]) {
+        PyErr_Clear();
+        for (int j = 0; j < 4; j++) Py_DECREF(out[j]);
+        return false;
+    }
+    return true;
+}
+
 // scan(bricks, field_cap, fptr, fsize, nfields, dims, le, re, mptr, msize)
-// bricks: sequence of (data, mask, left_edge, right_edge, dims) tuples.
+// bricks: sequence of (data, mask, left_edge, right_edge, dims) tuples or
+// PartitionedGrid-like objects.
 // The others are addresses of caller arrays: fptr (uint64) / fsize (int64)
 // of field_cap entries; nfields (int64), mptr (uint64), msize (int64; -1 for
 // no mask) of len(bricks) entries; dims (int64), le, re (float64) of
@@ -110,14 +148,15 @@ PyObject *scan(PyObject *, PyObject *args) {
     Py_ssize_t nfield = 0;
     bool ok = true;
     for (Py_ssize_t k = 0; ok && k < n; k++) {
-        PyObject *t = PySequence_Fast_GET_ITEM(seq, k);
-        if (!PyTuple_Check(t) || PyTuple_GET_SIZE(t) != 5) {
+        PyObject *part[5];
+        if (!brick_parts(PySequence_Fast_GET_ITEM(seq, k), part)) {
             ok = false;
             break;
         }
-        PyObject *data = PySequence_Fast(PyTuple_GET_ITEM(t, 0), "fields");
+        PyObject *data = PySequence_Fast(part[0], "fields");
         if (!data) {
             PyErr_Clear();
+            for (int i = 0; i < 5; i++) Py_DECREF(part[i]);
             ok = false;
             break;
         }
@@ -134,9 +173,12 @@ PyObject *scan(PyObject *, PyObject *args) {
             }
         }
         Py_DECREF(data);
-        if (!ok) break;
+        if (!ok) {
+            for (int i = 0; i < 5; i++) Py_DECREF(part[i]);
+            break;
+        }
         nf[k] = m;
-        PyObject *mask = PyTuple_GET_ITEM(t, 1);
+        PyObject *mask = part[1];
         if (mask == Py_None) {
             mptr[k] = 0;
             msz[k] = -1;
@@ -147,8 +189,9 @@ PyObject *scan(PyObject *, PyObject *args) {
             mptr[k] = p;
             msz[k] = c;
         }
-        ok = ok && three_doubles(PyTuple_GET_ITEM(t, 2), le + 3 * k) &&
-             three_doubles(PyTuple_GET_ITEM(t, 3), re + 3 * k) && three_ints(PyTuple_GET_ITEM(t, 4), dims + 3 * k);
+        ok = ok && three_doubles(part[2], le + 3 * k) && three_doubles(part[3], re + 3 * k) &&
+             three_ints(part[4], dims + 3 * k);
+        for (int i = 0; i < 5; i++) Py_DECREF(part[i]);
     }
     Py_DECREF(seq);
     if (!ok) Py_RETURN_FALSE;

@@ -28,7 +28,7 @@ import torch
 
 from . import _lib
 from . import transfer_functions as _tfm
-from .volume import BrickSet, render as _render
+from .volume import BrickSet, brick_parts, render as _render
 
 
 def _device():
@@ -101,13 +101,9 @@ def make_view(vp_pos, vp_dir, center, bounds, nx, ny, x_vec, y_vec, width, lens_
 
 
 def brick_tuple(pg):
-    """(data, mask, left_edge, right_edge, dims) of a PartitionedGrid -- yt's
-    own Cython object or :class:`yt_gb300.partitioned_grid.PartitionedGrid`.
-    dims come from the mask, which has one entry per cell."""
-    mask = pg.source_mask
-    if not isinstance(mask, np.ndarray):
-        mask = np.asarray(mask)
-    return list(pg.my_data), mask, pg.LeftEdge, pg.RightEdge, mask.shape
+    """(data, mask, left_edge, right_edge, dims) of a PartitionedGrid (yt's
+    own or :class:`yt_gb300.partitioned_grid.PartitionedGrid`)."""
+    return brick_parts(pg)
 
 
 class ImageSampler:
@@ -251,7 +247,9 @@ class ImageSampler:
             except BaseException as e:  # re-raised on the calling thread
                 checks["error"] = e
 
-        bricks = BrickSet([brick_tuple(pg) for pg in pending], device=dev, with_lo=self._with_lo)
+        # (with the device gather in flight: pending keeps the bricks alive
+        # and the stream is synchronised below before they may change)
+        bricks = BrickSet(pending, device=dev, with_lo=self._with_lo, sync=False)
         t1 = time.perf_counter()
         checker = threading.Thread(target=host_checks, daemon=True)
         checker.start()
@@ -260,8 +258,12 @@ class ImageSampler:
         px_pos = px_dir = None
         h2d = 0
         if self._px_pos is not None:
-            px_pos = torch.from_numpy(self._px_pos).to(dev)
-            px_dir = torch.from_numpy(self._px_dir).to(dev)
+            if bricks.direct:
+                # the kernel reads each pixel's ray from the host arrays
+                px_pos, px_dir = self._px_pos, self._px_dir
+            else:
+                px_pos = torch.from_numpy(self._px_pos).to(dev)
+                px_dir = torch.from_numpy(self._px_dir).to(dev)
             h2d += self._px_pos.nbytes + self._px_dir.nbytes
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -26,6 +26,16 @@ def _pinned(shape, dtype, device) -> torch.Tensor:
     return torch.empty(shape, dtype=dtype, pin_memory=torch.device(device).type == "cuda")
 
 
+def brick_parts(pg):
+    """(data, mask, left_edge, right_edge, dims) of a PartitionedGrid -- yt's
+    own Cython object or :class:`yt_gb300.partitioned_grid.PartitionedGrid`.
+    dims come from the mask, which has one entry per cell."""
+    mask = pg.source_mask
+    if not isinstance(mask, np.ndarray):
+        mask = np.asarray(mask)
+    return list(pg.my_data), mask, pg.LeftEdge, pg.RightEdge, mask.shape
+
+
 _MARSHAL: list = []
 
 
@@ -116,13 +126,20 @@ assert BRICK_DTYPE.itemsize == C.sizeof(_lib.Brick)
 
 
 class BrickSet:
-    """Bricks ``(data, mask, left_edge, right_edge, dims)`` resident on ``device``.
+    """Bricks ``(data, mask, left_edge, right_edge, dims)`` resident on ``device``
+    (PartitionedGrid objects are taken as well).
+
+    On a GPU that reads pageable host memory (``direct``, by default where
+    available) the device gathers the float64 fields itself; ``sync=False``
+    then returns with that gather in flight on the current stream, and the
+    caller keeps the bricks' arrays unchanged until the stream has passed
+    it.
 
     ``data`` is a list of float64 arrays (one per field, any shape; the
     samplers index them exactly as yt does), ``mask`` a uint8 array of
     ``dims`` or None (all ones)."""
 
-    def __init__(self, bricks: Sequence, device="cuda", with_lo=False, direct=None):
+    def __init__(self, bricks: Sequence, device="cuda", with_lo=False, direct=None, sync=True):
         self.device = torch.device(device)
         direct = device_reads_host(self.device) if direct is None else bool(direct)
         self.direct = direct
@@ -155,26 +172,6 @@ class BrickSet:
         fbrick = np.repeat(np.arange(n), nfields[:n])
         dst_f = (data_off[fbrick] + (np.arange(len(src)) - fstart[fbrick]) * stride[fbrick]).astype(np.int64)
         arena_len = max(total, 4)
-        if direct:
-            # the device reads the caller's float64 arrays over the CPU-GPU
-            # link and writes the float32 arena itself
-            buf = torch.empty((arena_len,), dtype=torch.float32, device=self.device)
-            buf_lo = torch.empty((arena_len,), dtype=torch.float32, device=self.device) if with_lo else None
-            stream = torch.cuda.current_stream(self.device)
-            _lib.check(L.ytgb_gather_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
-                                            buf.data_ptr(), buf_lo.data_ptr() if buf_lo is not None else None,
-                                            arena_len, C.c_void_p(stream.cuda_stream)), "ytgb_gather_fields")
-        else:
-            # float64 -> float32 gather into the pinned arena, on all host cores
-            buf = _pinned((arena_len,), torch.float32, self.device)
-            buf_lo = _pinned((arena_len,), torch.float32, self.device) if with_lo else None
-            if with_lo:
-                _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data,
-                                                    len(src), buf.data_ptr(), buf_lo.data_ptr(), 0),
-                           "ytgb_pack_fields_split")
-            else:
-                _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
-                                              buf.data_ptr(), 0), "ytgb_pack_fields")
         # masks: kept only when some cell is masked out
         mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
         desc["mask_offset"][:] = -1
@@ -193,15 +190,40 @@ class BrickSet:
                 desc["mask_offset"][mk_brick] = mdst
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
-        self.data = buf.to(self.device, non_blocking=True)
-        self.data_lo = buf_lo.to(self.device, non_blocking=True) if buf_lo is not None else None
-        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
+        # the small tables first: copies from pageable memory wait for the
+        # stream, which is idle before the gather below
         self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
         self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
+        self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
         if direct:
-            # the caller's arrays (and the converted copies in keep) may
-            # change or go once this returns: let the device finish reading
-            torch.cuda.current_stream(self.device).synchronize()
+            # the device reads the caller's float64 arrays over the CPU-GPU
+            # link and writes the float32 arena itself
+            buf = torch.empty((arena_len,), dtype=torch.float32, device=self.device)
+            buf_lo = torch.empty((arena_len,), dtype=torch.float32, device=self.device) if with_lo else None
+            stream = torch.cuda.current_stream(self.device)
+            _lib.check(L.ytgb_gather_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
+                                            buf.data_ptr(), buf_lo.data_ptr() if buf_lo is not None else None,
+                                            arena_len, C.c_void_p(stream.cuda_stream)), "ytgb_gather_fields")
+            self.data, self.data_lo = buf, buf_lo
+            # the device reads the caller's arrays (and converted copies) and
+            # the pointer lists asynchronously: with sync=False the caller
+            # keeps the bricks unchanged until the stream has passed here
+            self._gather_keep = (src, fsize, dst_f)
+            if sync:
+                stream.synchronize()
+        else:
+            # float64 -> float32 gather into the pinned arena, on all host cores
+            buf = _pinned((arena_len,), torch.float32, self.device)
+            buf_lo = _pinned((arena_len,), torch.float32, self.device) if with_lo else None
+            if with_lo:
+                _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data,
+                                                    len(src), buf.data_ptr(), buf_lo.data_ptr(), 0),
+                           "ytgb_pack_fields_split")
+            else:
+                _lib.check(L.ytgb_pack_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
+                                              buf.data_ptr(), 0), "ytgb_pack_fields")
+            self.data = buf.to(self.device, non_blocking=True)
+            self.data_lo = buf_lo.to(self.device, non_blocking=True) if buf_lo is not None else None
         self.nbytes = int(self.data.numel() * 4)
         self.upload_bytes = int(self.data.numel() * 4 * (2 if with_lo else 1) + self.bounds.numel() * 8 +
                                 self.desc.numel() + (self.masks.numel() if self.masks is not None else 0))
@@ -218,7 +240,8 @@ class BrickSet:
         fptr, fsz = [], []             # every field of every brick, in order
         mk_k, mptr, msz = [], [], []   # bricks with a mask
         addr = _address
-        for k, (data, mask, le_k, re_k, dims_k) in enumerate(bricks):
+        for k, item in enumerate(bricks):
+            data, mask, le_k, re_k, dims_k = item if isinstance(item, tuple) else brick_parts(item)
             dims_l.append(dims_k)
             le_l.append(le_k)
             re_l.append(re_k)
@@ -288,45 +311,27 @@ class BrickSet:
 
     def _layout(self, dims, le, re, nfields, sizes_min, sizes_max):
         """Descriptors, arena strides/offsets and cell-boundary tables of
-        bricks with the given geometry and per-field element counts."""
+        bricks with the given geometry and per-field element counts
+        (``ytgb_brick_layout``: PartitionedGrid.__cinit__'s dds and idds,
+        partitioned_grid.pyx:54-55, and the k*dds + le tables walk_volume
+        forms, grid_traversal.pyx:106-108, in the same float64 operations)."""
         n, m = self.n, max(self.n, 1)
         desc = np.zeros(m, dtype=BRICK_DTYPE)
         self.cells = dims.prod(axis=1)
         self.verts = (dims + 1).prod(axis=1)
         self.min_elems = np.zeros(m, dtype=np.int64)
         self.min_elems[:n] = sizes_min
-        stride = np.zeros(m, dtype=np.int64)
-        stride[:n] = (sizes_max + 3) & ~3
-        data_off = np.concatenate([[0], np.cumsum(stride * nfields)])[:m]
-        total = int((stride * nfields).sum())
-        # PartitionedGrid.__cinit__ (partitioned_grid.pyx:54-55), elementwise
-        dds = (re - le) / dims
-        idds = 1.0 / dds
-        desc["left_edge"] = le
-        desc["right_edge"] = re
-        desc["dds"] = dds
-        desc["idds"] = idds
-        desc["snap"] = 1e-10 * dds
-        desc["dims"] = dims
-        desc["n_fields"] = nfields
-        desc["data_offset"] = data_off
-        desc["field_stride"] = stride
-        desc["lef"] = le.astype(np.float32)
-        desc["ref"] = re.astype(np.float32)
-        desc["iddsf"] = idds.astype(np.float32)
-        # cell-boundary tables: for each brick and axis, k*dds + le for
-        # k = 0..dims (the float64 values walk_volume forms for tmax,
-        # grid_traversal.pyx:106-108); numpy's elementwise multiply and add
-        # round exactly like the reference's C expression
-        cnt = (dims + 1)[:n].ravel()
-        starts = np.concatenate([[0], np.cumsum(cnt)])
-        nb_total = int(starts[-1])
-        kk = np.arange(nb_total, dtype=np.float64) - np.repeat(starts[:-1], cnt)
-        bounds = kk * np.repeat(dds[:n].ravel(), cnt) + np.repeat(le[:n].ravel(), cnt)
-        desc["bounds_offset"][:n] = starts[:-1].reshape(n, 3)[:, 0] if n else []
-        if nb_total == 0:
-            bounds = np.zeros(1)
-        return desc, stride, data_off, total, bounds
+        nb_total = int((dims[:n] + 1).sum())
+        bounds = np.zeros(max(nb_total, 1))
+        total = C.c_int64(0)
+        if n:
+            smax = np.ascontiguousarray(sizes_max, dtype=np.int64)
+            _lib.check(_lib.lib().ytgb_brick_layout(
+                n, np.ascontiguousarray(dims[:n]).ctypes.data, np.ascontiguousarray(le[:n]).ctypes.data,
+                np.ascontiguousarray(re[:n]).ctypes.data, np.ascontiguousarray(nfields[:n]).ctypes.data,
+                smax.ctypes.data, desc.ctypes.data, bounds.ctypes.data, bounds.size, C.byref(total)),
+                "ytgb_brick_layout")
+        return desc, desc["field_stride"].copy(), desc["data_offset"].copy(), int(total.value), bounds
 
     def rects(self, view: _lib.View, order: np.ndarray) -> np.ndarray:
         """Per-order-entry pixel rectangles (ytgb_brick_rects)."""
@@ -384,7 +389,12 @@ def check_inputs(bricks: BrickSet, view: _lib.View, order, kind, image=None, zbu
         raise ValueError("zbuffer must be a contiguous float64 (nx, ny) tensor")
     if view.lens == _lib.LENS_PER_PIXEL:
         for t in (px_pos, px_dir):
-            if t is None or t.numel() != nx * ny * 3 or t.dtype != torch.float64 or not t.is_contiguous():
+            if isinstance(t, np.ndarray):
+                if t.size != nx * ny * 3 or t.dtype != np.float64 or not t.flags.c_contiguous:
+                    raise ValueError("per-pixel lens needs contiguous float64 (nx, ny, 3) positions and directions")
+                if not device_reads_host(bricks.device):
+                    raise ValueError("host per-pixel ray arrays need a device that reads pageable host memory")
+            elif t is None or t.numel() != nx * ny * 3 or t.dtype != torch.float64 or not t.is_contiguous():
                 raise ValueError("per-pixel lens needs contiguous float64 (nx, ny, 3) positions and directions")
 
 
@@ -417,8 +427,9 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
     args.flags = int(flags)
     args.view = view
     if px_pos is not None:
-        args.view.px_pos = px_pos.data_ptr()
-        args.view.px_dir = px_dir.data_ptr()
+        # device tensors, or host arrays the device reads in place
+        args.view.px_pos = px_pos.ctypes.data if isinstance(px_pos, np.ndarray) else px_pos.data_ptr()
+        args.view.px_dir = px_dir.ctypes.data if isinstance(px_dir, np.ndarray) else px_dir.data_ptr()
     args.bricks = bricks.desc.data_ptr()
     args.rects = tab_d.data_ptr()
     args.order = tab_d.data_ptr() + 4 * 4 * order.size
