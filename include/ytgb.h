@@ -286,6 +286,14 @@ int ytgb_pack_fields_split(const double *const *src, const int64_t *count, const
  * nothing, on a device without pageable memory access. */
 int ytgb_gather_fields(const double *const *src, const int64_t *count, const int64_t *dst_offset, int64_t n,
                        float *d_arena, float *d_arena_lo, int64_t arena_len, void *stream);
+/* The masks' counterpart of ytgb_gather_fields: the device copies the host
+ * uint8 masks src[k] (count[k] bytes, of brick brick[k]) to d_masks +
+ * dst_offset[k] and sets d_desc[brick[k]].mask_offset = dst_offset[k] for a
+ * brick with any byte other than 1 (descriptors keep -1, all ones,
+ * otherwise).  Host arrays read by the device, as for ytgb_gather_fields. */
+int ytgb_gather_masks(const uint8_t *const *src, const int64_t *count, const int64_t *dst_offset,
+                      const int32_t *brick, int64_t n, uint8_t *d_masks, int64_t masks_len, ytgb_brick *d_desc,
+                      int32_t n_bricks, void *stream);
 /* *out = 1 when the current device reads pageable host memory coherently
  * (the condition of ytgb_gather_fields), else 0. */
 int ytgb_device_reads_host(int32_t *out);

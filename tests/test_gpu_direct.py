@@ -126,3 +126,37 @@ def test_sampler_rerenders_when_inputs_are_not_default(cuda, case):
                                       zbuffer=None if case == "image" else zb, image=init)
     assert relative_error(out, ref, channels=(0, 1, 2))[0] <= 1e-5
     assert int(s.last_counters[0]) == visits
+
+
+def test_direct_masks_match_host_pack(cuda):
+    """Masks with cells switched off: the device gather marks the same bricks
+    (mask_offset) and copies the same bytes as the host check and pack, and
+    both render the same image bit for bit."""
+    if not device_reads_host(cuda):
+        pytest.skip("the device does not read pageable host memory")
+    from yt_gb300.render import Renderer
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=48)
+    rng = np.random.default_rng(2)
+    bricks = []
+    for k, (data, mask, le, re, dims) in enumerate(w.bricks):
+        shape = tuple(int(d) for d in dims)
+        m = np.ones(shape, np.uint8) if k % 3 else (rng.random(shape) < 0.8).astype(np.uint8)
+        bricks.append((data, m, le, re, dims))
+    a = BrickSet(bricks, device=cuda, direct=False)
+    b = BrickSet(bricks, device=cuda, direct=True)
+    da = a.desc.cpu().numpy().view(a.desc_host.dtype)
+    db = b.desc.cpu().numpy().view(b.desc_host.dtype)
+    # the host path keeps every mask once one is not all ones; the device
+    # marks only the bricks whose mask is not: the same cells are sampled
+    ma, mb = a.masks.cpu().numpy(), b.masks.cpu().numpy()
+    assert (db["mask_offset"] >= 0).sum() > 0
+    for oa, ob, c in zip(da["mask_offset"], db["mask_offset"], a.cells):
+        if ob >= 0:
+            assert oa == ob and np.array_equal(ma[oa: oa + c], mb[ob: ob + c]) and (mb[ob: ob + c] != 1).any()
+        elif oa >= 0:
+            assert (ma[oa: oa + c] == 1).all()
+    cam = w.views[0].camera
+    ia = Renderer(a, w.tf, device=cuda, kdtree=w.kdtree).render(cam).cpu().numpy()
+    ib = Renderer(b, w.tf, device=cuda, kdtree=w.kdtree).render(cam).cpu().numpy()
+    assert np.abs(ia).max() > 0 and np.array_equal(ia.view(np.int64), ib.view(np.int64))

@@ -199,6 +199,8 @@ SIGNATURES = {
     "ytgb_gather_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                      C.c_int64, C.c_void_p]),
     "ytgb_device_reads_host": (C.c_int, [C.c_void_p]),
+    "ytgb_gather_masks": (C.c_int, [C.c_void_p] * 4 + [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
+                                                        C.c_void_p]),
     "ytgb_brick_layout": (C.c_int, [C.c_int64] + [C.c_void_p] * 7 + [C.c_int64, C.c_void_p]),
     "ytgb_trace_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_pack_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),

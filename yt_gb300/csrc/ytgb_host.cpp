@@ -7,6 +7,7 @@
 #include <cstring>
 #include <climits>
 #include <string>
+#include <thread>
 #include <vector>
 #include <algorithm>
 
@@ -190,21 +191,39 @@ extern "C" int ytgb_brick_rects(const ytgb_view *view, const ytgb_brick *bricks,
         return YTGB_ERR_INVALID;
     }
     for (int32_t k = 0; k < n_order; k++) {
-        int32_t b = order ? order[k] : k;
+        const int32_t b = order ? order[k] : k;
         if (b < 0 || b >= n_bricks) {
             ytgb_set_error("ytgb_brick_rects: order entry out of range");
             return YTGB_ERR_INVALID;
         }
-        int64_t it[4];
-        if (view->extent == YTGB_EXTENT_PLANE_PARALLEL) extent_plane_parallel(view, &bricks[b], it);
-        else if (view->extent == YTGB_EXTENT_PERSPECTIVE) extent_perspective(view, &bricks[b], it);
-        else { it[0] = 0; it[1] = view->nx; it[2] = 0; it[3] = view->ny; }
-        it[0] = i64clip(it[0] - 1, 0, view->nx);
-        it[1] = i64clip(it[1] + 1, 0, view->nx);
-        it[2] = i64clip(it[2] - 1, 0, view->ny);
-        it[3] = i64clip(it[3] + 1, 0, view->ny);
-        for (int q = 0; q < 4; q++) rects[4 * k + q] = (int32_t)it[q];
     }
+    auto run = [&](int32_t k0, int32_t k1) {
+        for (int32_t k = k0; k < k1; k++) {
+            const int32_t b = order ? order[k] : k;
+            int64_t it[4];
+            if (view->extent == YTGB_EXTENT_PLANE_PARALLEL) extent_plane_parallel(view, &bricks[b], it);
+            else if (view->extent == YTGB_EXTENT_PERSPECTIVE) extent_perspective(view, &bricks[b], it);
+            else { it[0] = 0; it[1] = view->nx; it[2] = 0; it[3] = view->ny; }
+            it[0] = i64clip(it[0] - 1, 0, view->nx);
+            it[1] = i64clip(it[1] + 1, 0, view->nx);
+            it[2] = i64clip(it[2] - 1, 0, view->ny);
+            it[3] = i64clip(it[3] + 1, 0, view->ny);
+            for (int q = 0; q < 4; q++) rects[4 * k + q] = (int32_t)it[q];
+        }
+    };
+    // the bricks are independent: up to 8 host threads, 128 bricks or more each
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int threads = std::max(1, std::min({8, hw > 0 ? hw : 1, n_order / 128}));
+    if (threads == 1) {
+        run(0, n_order);
+        return YTGB_OK;
+    }
+    std::vector<std::thread> pool;
+    const int32_t step = (n_order + threads - 1) / threads;
+    for (int t = 1; t < threads; t++)
+        pool.emplace_back(run, std::min(n_order, t * step), std::min(n_order, (t + 1) * step));
+    run(0, std::min(n_order, step));
+    for (auto &th : pool) th.join();
     return YTGB_OK;
 }
 

@@ -93,6 +93,27 @@ gather_fields_kernel(const double *const *src, const int64_t *count, const int64
     }
 }
 
+// One block per mask (grid-stride): the host uint8 cell mask into the mask
+// arena; a brick with any byte other than 1 gets its mask_offset (it stays
+// -1, "all ones", otherwise: VolumeRenderSampler samples a cell when its
+// mask byte is 1, image_samplers.pyx:467-470).
+__global__ void __launch_bounds__(GATHER_BLOCK)
+gather_masks_kernel(const uint8_t *const *src, const int64_t *count, const int64_t *dst_offset, const int32_t *brick,
+                    int64_t n, uint8_t *masks, ytgb_brick *desc) {
+    for (int64_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint8_t *s = src[k];
+        const int64_t c = count[k];
+        uint8_t *d = masks + dst_offset[k];
+        int other = 0;
+        for (int64_t i = threadIdx.x; i < c; i += GATHER_BLOCK) {
+            const uint8_t v = s[i];
+            d[i] = v;
+            other |= v != 1;
+        }
+        if (__syncthreads_or(other) && threadIdx.x == 0) desc[brick[k]].mask_offset = dst_offset[k];
+    }
+}
+
 bool device_reads_host() {
     int dev = 0, pma = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
@@ -140,6 +161,41 @@ extern "C" int ytgb_gather_fields(const double *const *src, const int64_t *count
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         ytgb_set_error(std::string("ytgb_gather_fields: ") + cudaGetErrorString(e));
+        return YTGB_ERR_CUDA;
+    }
+    return YTGB_OK;
+}
+
+extern "C" int ytgb_gather_masks(const uint8_t *const *src, const int64_t *count, const int64_t *dst_offset,
+                                 const int32_t *brick, int64_t n, uint8_t *d_masks, int64_t masks_len,
+                                 ytgb_brick *d_desc, int32_t n_bricks, void *stream) {
+    if (n < 0 || masks_len < 0 || (n > 0 && (!src || !count || !dst_offset || !brick || !d_masks || !d_desc))) {
+        ytgb_set_error("ytgb_gather_masks: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    if (n == 0) return YTGB_OK;
+    if (!device_reads_host()) {
+        ytgb_set_error("ytgb_gather_masks: the device cannot read pageable host memory");
+        return YTGB_ERR_INVALID;
+    }
+    if ((uintptr_t)d_desc & 7) {
+        ytgb_set_error("ytgb_gather_masks: misaligned descriptors");
+        return YTGB_ERR_INVALID;
+    }
+    for (int64_t k = 0; k < n; k++) {
+        if (count[k] < 0 || (count[k] > 0 && !src[k]) || dst_offset[k] < 0 || dst_offset[k] > masks_len - count[k] ||
+            brick[k] < 0 || brick[k] >= n_bricks) {
+            ytgb_set_error("ytgb_gather_masks: mask " + std::to_string(k) + " is null, does not fit the arena or "
+                           "names no brick");
+            return YTGB_ERR_INVALID;
+        }
+    }
+    const int blocks = (int)(n < 152 * 16 ? n : 152 * 16);
+    gather_masks_kernel<<<blocks, GATHER_BLOCK, 0, (cudaStream_t)stream>>>(src, count, dst_offset, brick, n, d_masks,
+                                                                          d_desc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ytgb_set_error(std::string("ytgb_gather_masks: ") + cudaGetErrorString(e));
         return YTGB_ERR_CUDA;
     }
     return YTGB_OK;

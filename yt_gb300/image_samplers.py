@@ -251,9 +251,11 @@ class ImageSampler:
         # and the stream is synchronised below before they may change)
         bricks = BrickSet(pending, device=dev, with_lo=self._with_lo, sync=False)
         t1 = time.perf_counter()
+        order = np.arange(len(pending), dtype=np.int32)
+        # the pixel rectangles on all cores before the checks take them
+        rects = bricks.rects(self._view, order)
         checker = threading.Thread(target=host_checks, daemon=True)
         checker.start()
-        order = np.arange(len(pending), dtype=np.int32)
         nx, ny = self.nv
         px_pos = px_dir = None
         h2d = 0
@@ -273,7 +275,7 @@ class ImageSampler:
         def launch(image_d, zb_d):
             _render(bricks, self._view, order, self.kind, image_d, tf=self._tf(), zbuffer=zb_d,
                     n_samples=self.n_samples, flags=self.flags, counters=counters, error=error,
-                    px_pos=px_pos, px_dir=px_dir, light=self._light(), keep=keep)
+                    px_pos=px_pos, px_dir=px_dir, light=self._light(), keep=keep, rects=rects)
 
         image_d = torch.zeros((nx, ny, 4), dtype=torch.float64, device=dev)
         try:

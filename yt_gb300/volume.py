@@ -176,7 +176,12 @@ class BrickSet:
         mstart = np.concatenate([[0], np.cumsum(self.cells[:n])]).astype(np.int64)
         desc["mask_offset"][:] = -1
         mbuf = None
-        if mk_brick.size:
+        mask_gather = None
+        if mk_brick.size and direct:
+            # the device copies the masks and marks the bricks that need one
+            mask_gather = (np.ascontiguousarray(mptr, dtype=np.uintp), np.ascontiguousarray(mk_size, dtype=np.int64),
+                           np.ascontiguousarray(mstart[mk_brick]), np.ascontiguousarray(mk_brick, dtype=np.int32))
+        elif mk_brick.size:
             msrc = np.ascontiguousarray(mptr, dtype=np.uintp)
             mcnt = np.ascontiguousarray(mk_size, dtype=np.int64)
             mdst = np.ascontiguousarray(mstart[mk_brick])
@@ -195,6 +200,14 @@ class BrickSet:
         self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
         self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
         self.masks = mbuf.to(self.device, non_blocking=True) if mbuf is not None else None
+        if mask_gather is not None:
+            msrc, mcnt, mdst, mbrick = mask_gather
+            mlen = max(int(mstart[-1]), 1)
+            self.masks = torch.empty((mlen,), dtype=torch.uint8, device=self.device)
+            stream = torch.cuda.current_stream(self.device)
+            _lib.check(L.ytgb_gather_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, mbrick.ctypes.data,
+                                           mbrick.size, self.masks.data_ptr(), mlen, self.desc.data_ptr(), n,
+                                           C.c_void_p(stream.cuda_stream)), "ytgb_gather_masks")
         if direct:
             # the device reads the caller's float64 arrays over the CPU-GPU
             # link and writes the float32 arena itself
@@ -208,7 +221,7 @@ class BrickSet:
             # the device reads the caller's arrays (and converted copies) and
             # the pointer lists asynchronously: with sync=False the caller
             # keeps the bricks unchanged until the stream has passed here
-            self._gather_keep = (src, fsize, dst_f)
+            self._gather_keep = (src, fsize, dst_f, mask_gather)
             if sync:
                 stream.synchronize()
         else:
