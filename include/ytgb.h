@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define YTGB_ABI_VERSION 2
+#define YTGB_ABI_VERSION 3
 
 #define YTGB_OK 0
 #define YTGB_ERR_INVALID (-1)   /* bad argument, detected on the host */
@@ -342,6 +342,11 @@ typedef struct ytgb_octree_args {
     int32_t pad;
     double dle[3];
     double dre[3];
+    /* optional (NULL: not used): per cell 12 floats -- the left edge split
+     * into float32 high and low parts (3 + 3), (float)(1/(right - left)) (3),
+     * 3 unused -- from which the samplers form each cell's entry point in
+     * float32 pairs instead of float64 (16-byte aligned) */
+    const float *edges_f;
 } ytgb_octree_args;
 
 /* Replaces _OctreeRayTracing(LE, RE, depth).add_nodes(ipos, lvl, key)

@@ -169,6 +169,7 @@ static int run_octree(const ytgb_render_args &a, const ytgb_octree_args &oa, uns
     o.n_nodes = oa.n_nodes;
     o.verts = oa.verts;
     o.edges = oa.edges;
+    o.edges_f = reinterpret_cast<const float4 *>(oa.edges_f);
     o.n_cells = oa.n_cells;
     o.depth = oa.depth;
     for (int i = 0; i < 3; i++) {

@@ -300,7 +300,7 @@ def test_light_source_amr(emu):
     check(emu, w.bricks, cam, w.order(cam), _lib.LIGHT_SOURCE, tf=w.tf, light=LIGHT_CASES[1])
 
 
-def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None, rays=None):
+def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None, rays=None, float_edges=True):
     """The octree path on the CPU harness and on the oracle, same inputs
     (``rays``: per-pixel (positions, directions) replacing the camera's)."""
     from yt_gb300.octree import ONODE_DTYPE, Octree
@@ -314,6 +314,13 @@ def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None, rays=None):
     edges = np.ascontiguousarray(np.concatenate([le, re, 1 / (re - le)], axis=1))
     o = _lib.OctreeArgs()
     o.nodes, o.verts, o.edges = nodes.ctypes.data, verts.ctypes.data, edges.ctypes.data
+    if float_edges:
+        leh = le.astype(np.float32)
+        edges_f = np.zeros((cells.shape[0], 12), dtype=np.float32)
+        edges_f[:, 0:3] = leh
+        edges_f[:, 3:6] = (le - leh.astype(np.float64)).astype(np.float32)
+        edges_f[:, 6:9] = (1 / (re - le)).astype(np.float32)
+        o.edges_f = edges_f.ctypes.data
     o.n_nodes, o.n_cells, o.depth = nodes.size, cells.shape[0], depth
     for i in range(3):
         o.dle[i], o.dre[i] = 0.0, 1.0
@@ -363,9 +370,10 @@ def run_octree_both(L, kind, cam, tf=None, ns=1, seed=2, light=None, rays=None):
     return img, cnt, h.reshape(nx, ny), c.reshape(nx, ny), ref, visits, hr, cr, cells
 
 
+@pytest.mark.parametrize("float_edges", [True, False])
 @pytest.mark.parametrize("kind", [_lib.VOLUME_RENDER, _lib.PROJECTION, _lib.INTERPOLATED_PROJECTION, _lib.MIP,
                                   _lib.LIGHT_SOURCE])
-def test_octree_path(emu, kind):
+def test_octree_path(emu, kind, float_edges):
     """cast_through_octree: traversal (cell keys, enter/exit t bits) bit for
     bit against the oracle (itself pinned to the compiled reference), images
     within 1e-5, for every sampler."""
@@ -379,7 +387,8 @@ def test_octree_path(emu, kind):
             tf.add_gaussian(loc, wd, list(rgba))
     light = ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0)) if kind == _lib.LIGHT_SOURCE else None
     for ns in ((1, 2) if kind in (_lib.VOLUME_RENDER, _lib.INTERPOLATED_PROJECTION) else (1,)):
-        img, cnt, h, c, ref, visits, hr, cr, _ = run_octree_both(emu, kind, cam, tf, ns, light=light)
+        img, cnt, h, c, ref, visits, hr, cr, _ = run_octree_both(emu, kind, cam, tf, ns, light=light,
+                                                                 float_edges=float_edges)
         assert np.array_equal(c, cr) and np.array_equal(h, hr)
         assert int(cnt[0]) == visits and visits > 0
         mx, rms = relative_error(img, ref, channels=(0, 1, 2) if tf is not None else (0,))

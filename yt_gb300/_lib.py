@@ -126,6 +126,7 @@ class OctreeArgs(C.Structure):
         ("pad", C.c_int32),
         ("dle", C.c_double * 3),
         ("dre", C.c_double * 3),
+        ("edges_f", C.c_void_p),
     ]
 
 
@@ -234,7 +235,7 @@ def lib() -> C.CDLL:
                 fn = getattr(L, name)
                 fn.restype = res
                 fn.argtypes = args
-            if L.ytgb_abi_version() != 2:
+            if L.ytgb_abi_version() != 3:
                 raise YtgbError("libytgb ABI version mismatch")
             _lib = L
     return _lib

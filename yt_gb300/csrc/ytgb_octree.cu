@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(OBLOCK) octree_kernel(const ytgb_render_args a
         o.n_nodes = oa.n_nodes;
         o.verts = oa.verts;
         o.edges = oa.edges;
+        o.edges_f = reinterpret_cast<const float4 *>(oa.edges_f);
         o.n_cells = oa.n_cells;
         o.depth = oa.depth;
         for (int i = 0; i < 3; i++) {
@@ -125,7 +126,7 @@ int octree_checks(const ytgb_render_args *a, const ytgb_octree_args *o, bool tra
         return YTGB_ERR_INVALID;
     }
     auto mis = [](const void *q, uintptr_t al) { return q && ((uintptr_t)q & (al - 1)) != 0; };
-    if (mis(o->nodes, 8) || mis(o->verts, 4) || mis(o->edges, 8) || mis(a->image, 8) || mis(a->tf_tables, 16) ||
+    if (mis(o->nodes, 8) || mis(o->verts, 4) || mis(o->edges, 8) || mis(o->edges_f, 16) || mis(a->image, 8) || mis(a->tf_tables, 16) ||
         mis(a->counters, 8) || mis(a->error, 4) || mis(v.px_pos, 8) || mis(v.px_dir, 8) || mis(a->data_lo, 4)) {
         ytgb_set_error("ytgb_render_octree: misaligned pointer");
         return YTGB_ERR_INVALID;

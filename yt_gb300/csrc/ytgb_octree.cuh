@@ -29,6 +29,7 @@ struct OctreeView {
     int32_t n_nodes;
     const float *verts;    // 8 per cell, (i,j,k) C order
     const double *edges;   // 9 per cell: left edge, right edge, 1/(right - left)
+    const float4 *edges_f; // 3 per cell (or null): left edge hi, lo, (float)(1/(right - left))
     int32_t n_cells;
     int32_t depth;
     double dle[3], dre[3], size[3];
@@ -71,6 +72,13 @@ YTGB_HD int next_node(double tx, double ty, double tz, int ix, int iy, int iz) {
     if (lt<K>(tx, smin<K>(ty, tz))) return ix;
     if (lt<K>(ty, smin<K>(tx, tz))) return iy;
     return iz;
+}
+
+// s + e == a + b exactly (TwoSum, Knuth TAOCP vol. 2, 4.2.2)
+YTGB_HD void two_sum(float a, float b, float &s, float &e) {
+    s = fadd(a, b);
+    const float bp = fsub(s, a);
+    e = fadd(fsub(a, fsub(s, bp)), fsub(b, bp));
 }
 
 struct OFrame {
@@ -212,6 +220,15 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
     // the in-cell position), so a product with 1/len (within an ulp of the
     // quotient) serves it; the trace keeps the reference's exact quotients.
     const double ilen = ddiv(1.0, len);
+    // the ray as float32 pairs (hi + lo = the float64 value to ~2^-48)
+    float ph[3], pl[3], dh[3], dl[3];
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        ph[i] = (float)r.pos[i];
+        pl[i] = (float)dsub(r.pos[i], (double)ph[i]);
+        dh[i] = (float)r.dir[i];
+        dl[i] = (float)dsub(r.dir[i], (double)dh[i]);
+    }
     return octree_cast(o, r.pos, r.dir, [&](int key, double t_in, double t_out) {
         if (key < 0 || key >= o.n_cells) {
             st.guarded++;
@@ -230,7 +247,6 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
             st.visits++;
             return;
         }
-        const double *ed = o.edges + 9ll * key;
         CellCtx c;
         c.base = o.verts + 8ll * key;
         c.fstride = 0;
@@ -239,13 +255,42 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
         c.sx = 4;
         c.sy = 2;
         float P[3];
-        YTGB_UNROLL
-        for (int i = 0; i < 3; i++) {
-            c.dims[i] = 1;
-            const double idds = ldg(ed + 6 + i);
-            c.vel[i] = fmul(r.fdir[i], (float)idds);
-            // (enter * v_dir + v_pos - left_edge) * idds (image_samplers.pyx:475-478)
-            P[i] = (float)dmul(dsub(dadd(dmul(e, r.dir[i]), r.pos[i]), ldg(ed + i)), idds);
+        if (o.edges_f) {
+            // (enter * v_dir + v_pos - left_edge) * idds (image_samplers.pyx:
+            // 475-478) in float32 pairs: the products exact by FMA, the sums
+            // by TwoSum, so the difference keeps ~2^-48 of the operands' scale
+            // (the cell is ~2^-9 of it), then one float32 rounding and the
+            // float32 idds: within a float32 ulp or two of the float64 form,
+            // on the float32 pipes rather than six float64 operations
+            const float4 A = ldg(o.edges_f + 3ll * key), B = ldg(o.edges_f + 3ll * key + 1);
+            const float4 D = ldg(o.edges_f + 3ll * key + 2);
+            const float leh[3] = {A.x, A.y, A.z}, lel[3] = {A.w, B.x, B.y}, idf[3] = {B.z, B.w, D.x};
+            const float eh = (float)e, el = (float)dsub(e, (double)eh);
+            YTGB_UNROLL
+            for (int i = 0; i < 3; i++) {
+                c.dims[i] = 1;
+                c.vel[i] = fmul(r.fdir[i], idf[i]);
+                const float mh = fmul(eh, dh[i]);
+                float ml = ffma(eh, dh[i], -mh);
+                ml = ffma(eh, dl[i], ml);
+                ml = ffma(el, dh[i], ml);
+                float sh, se, uh, ue;
+                two_sum(mh, ph[i], sh, se);
+                const float sl = fadd(fadd(se, ml), pl[i]);
+                two_sum(sh, -leh[i], uh, ue);
+                const float ul = fsub(fadd(ue, sl), lel[i]);
+                P[i] = fmul(fadd(uh, ul), idf[i]);
+            }
+        } else {
+            const double *ed = o.edges + 9ll * key;
+            YTGB_UNROLL
+            for (int i = 0; i < 3; i++) {
+                c.dims[i] = 1;
+                const double idds = ldg(ed + 6 + i);
+                c.vel[i] = fmul(r.fdir[i], (float)idds);
+                // (enter * v_dir + v_pos - left_edge) * idds (image_samplers.pyx:475-478)
+                P[i] = (float)dmul(dsub(dadd(dmul(e, r.dir[i]), r.pos[i]), ldg(ed + i)), idds);
+            }
         }
         const int cur[3] = {0, 0, 0};
         st.walks++;

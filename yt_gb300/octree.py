@@ -75,7 +75,9 @@ class OctreeVolume:
     """An octree and its cells resident on the device.  ``cells`` is yt's
     (n, 14) float64 layout: 8 vertex values ((i,j,k) C order), left edge,
     right edge; here split into float32 vertex values and float64 edges with
-    ``1/(right - left)`` precomputed as cast_through_octree computes it."""
+    ``1/(right - left)`` precomputed as cast_through_octree computes it, and a
+    float32 copy (left edge as high and low parts, 1/(right - left)) from
+    which the samplers form each cell's entry point."""
 
     def __init__(self, octree: Octree, cells, device="cuda"):
         self.device = torch.device(device)
@@ -86,19 +88,29 @@ class OctreeVolume:
         if keys.size and (keys.min() < 0 or keys.max() >= cells.shape[0]):
             raise ValueError("an octree key is not a row of the cell array")
         le, re = cells[:, 8:11], cells[:, 11:14]
-        edges = np.concatenate([le, re, 1 / (re - le)], axis=1)
+        idds = 1 / (re - le)
+        edges = np.concatenate([le, re, idds], axis=1)
+        # per cell: the left edge as float32 high and low parts, (float)idds
+        leh = le.astype(np.float32)
+        edges_f = np.zeros((cells.shape[0], 12), dtype=np.float32)
+        edges_f[:, 0:3] = leh
+        edges_f[:, 3:6] = (le - leh.astype(np.float64)).astype(np.float32)
+        edges_f[:, 6:9] = idds.astype(np.float32)
         self.n_cells = cells.shape[0]
         self.n_nodes = nodes.size
         self.nodes = torch.from_numpy(nodes.view(np.uint8).copy()).to(self.device)
         self.verts = torch.from_numpy(cells[:, :8].astype(np.float32)).to(self.device).reshape(-1)
         self.edges = torch.from_numpy(np.ascontiguousarray(edges)).to(self.device).reshape(-1)
-        self.upload_bytes = int(self.nodes.numel() + self.verts.numel() * 4 + self.edges.numel() * 8)
+        self.edges_f = torch.from_numpy(edges_f).to(self.device).reshape(-1)
+        self.upload_bytes = int(self.nodes.numel() + self.verts.numel() * 4 + self.edges.numel() * 8 +
+                                self.edges_f.numel() * 4)
 
     def args(self) -> _lib.OctreeArgs:
         o = _lib.OctreeArgs()
         o.nodes = self.nodes.data_ptr()
         o.verts = self.verts.data_ptr()
         o.edges = self.edges.data_ptr()
+        o.edges_f = self.edges_f.data_ptr()
         o.n_nodes = self.n_nodes
         o.n_cells = self.n_cells
         o.depth = self.octree.depth
