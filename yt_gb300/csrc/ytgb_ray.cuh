@@ -190,37 +190,35 @@ YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
 // the float64 add.
 struct AxisStep {
     long long bits;  // the float64 bits of tmax
-    long long q;
-    long long end;   // first bit pattern of the next binade
-    int mode;        // 0 round down, 1 round up, 2 half (to even), 3 float64 add
+    long long inc;   // ulps per add: q, plus one when the discarded part exceeds half an ulp
+    int ex;          // the exponent field of bits: the binade
+    int mode;        // 0 fixed increment, 2 exact half (to even), 3 float64 add
 };
 
 YTGB_HD void step_prepare(AxisStep &s, double d) {
     const long long xb = s.bits, db = dbits(d);
     const int ex = (int)(xb >> 52), ed = (int)(db >> 52);
-    s.end = (long long)(ex + 1) << 52;
-    s.q = 0;
+    s.ex = ex;
+    s.inc = 0;
     if (xb <= 0 || db <= 0 || ex == 0 || ed == 0 || ex >= 2046 || ed >= 2047 || ed >= ex) {
         s.mode = 3;
         return;
     }
     const int sh = ex - ed;
-    if (sh >= 64) {
-        s.mode = 0;
-        return;
-    }
+    s.mode = 0;
+    if (sh >= 64) return;
     const unsigned long long md = (unsigned long long)((db & MANT52) | (1LL << 52));
-    s.q = (long long)(md >> sh);
+    const long long q = (long long)(md >> sh);
     const unsigned long long r = md & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    s.mode = r < half ? 0 : (r > half ? 1 : 2);
+    s.inc = r > half ? q + 1 : q;
+    if (r == half) s.mode = 2;
 }
 
 YTGB_HD void step_advance(AxisStep &s, double d) {
     if (s.mode != 3) {
-        long long inc = s.q + (s.mode == 1 ? 1 : 0);
-        if (s.mode == 2) inc += (s.bits + s.q) & 1;
-        const long long nb = s.bits + inc;
-        if (nb < s.end) {
+        long long nb = s.bits + s.inc;
+        if (s.mode == 2) nb += nb & 1;  // a tie: to the even neighbour
+        if ((int)(nb >> 52) == s.ex) {
             s.bits = nb;
             return;
         }
