@@ -81,9 +81,9 @@ __global__ void __launch_bounds__(OBLOCK) octree_kernel(const ytgb_render_args a
         }
     }
     if (a.counters) {
-        if (st.visits) atomicAdd(&s_cnt[0], st.visits);
-        if (st.walks) atomicAdd(&s_cnt[1], st.walks);
-        if (st.guarded) atomicAdd(&s_cnt[3], st.guarded);
+        if (st.visits) atomicAdd(&s_cnt[0], (unsigned long long)st.visits);
+        if (st.walks) atomicAdd(&s_cnt[1], (unsigned long long)st.walks);
+        if (st.guarded) atomicAdd(&s_cnt[3], (unsigned long long)st.guarded);
         if (active) atomicAdd(&s_cnt[2], 1ull);
         __syncthreads();
         if (tid < 4 && s_cnt[tid]) atomicAdd(a.counters + tid, s_cnt[tid]);

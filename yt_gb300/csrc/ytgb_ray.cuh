@@ -656,12 +656,9 @@ struct RayState {
     unsigned touched;            // channels the sampler wrote
     unsigned long long th;       // trace hash
     long long tcount;            // trace count
-    unsigned long long visits, walks, guarded;
-    double tdelta[3];            // cached per dds
-    long long last_dds[3];
-    double max_t;
+    unsigned visits, walks, guarded;  // per ray (summed into 64-bit counters)
+    double max_t;  // (its key dkey(max_t) is recomputed per walk)
     float max_tf;
-    long long kmax;
     bool comp;
 };
 
@@ -671,7 +668,6 @@ YTGB_HD void ray_state_init(RayState &s, const double *img, double zbuf, bool ha
     max_t = max_t < 1.0 ? max_t : 1.0;  // also grid_traversal.pyx:42
     s.max_t = max_t;
     s.max_tf = (float)max_t;
-    s.kmax = dkey(max_t);
     YTGB_UNROLL
     for (int c = 0; c < 4; c++) {
         double x0 = img ? img[c] : 0.0;
@@ -682,11 +678,6 @@ YTGB_HD void ray_state_init(RayState &s, const double *img, double zbuf, bool ha
     s.th = 0;
     s.tcount = 0;
     s.visits = s.walks = s.guarded = 0;
-    YTGB_UNROLL
-    for (int i = 0; i < 3; i++) {
-        s.tdelta[i] = 0.0;
-        s.last_dds[i] = -1;
-    }
     s.comp = !(flags & YTGB_FLAG_NO_COMPENSATION);
 }
 
@@ -887,19 +878,13 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     load_brick_f(bp, bf);
     if (surely_misses(bf, r, st.max_tf)) return;
     const double max_t = st.max_t;
-    const long long kmax = st.kmax;
+    const long long kmax = dkey(st.max_t);
     Walk w;
     if (!walk_setup(bf, bp, a.bounds, r, max_t, kmax, w)) return;
-    // tdelta depends on the ray and dds only (grid_traversal.pyx:86)
+    // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
+    double tdelta[3];
     YTGB_UNROLL
-    for (int i = 0; i < 3; i++) {
-        const double dds = ldg(&bp->dds[i]);
-        const long long db = dbits(dds);
-        if (db != st.last_dds[i]) {
-            st.tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), dds);
-            st.last_dds[i] = db;
-        }
-    }
+    for (int i = 0; i < 3; i++) tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), ldg(&bp->dds[i]));
     st.walks++;
     CellCtx c;
     c.nf = ldg(&bp->n_fields);
@@ -923,9 +908,9 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
         A0.bits = b0;
         A1.bits = b1;
         A2.bits = b2;
-        step_prepare(A0, st.tdelta[0]);
-        step_prepare(A1, st.tdelta[1]);
-        step_prepare(A2, st.tdelta[2]);
+        step_prepare(A0, tdelta[0]);
+        step_prepare(A1, tdelta[1]);
+        step_prepare(A2, tdelta[2]);
         long long eb = dbits(w.enter_t);
         while (true) {
             if (++hitc > step_limit) {
@@ -945,17 +930,17 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
             int ci, di;
             if (i == 0) {
                 w.cur[0] += si;
-                step_advance(A0, st.tdelta[0]);
+                step_advance(A0, tdelta[0]);
                 ci = w.cur[0];
                 di = c.dims[0];
             } else if (i == 1) {
                 w.cur[1] += si;
-                step_advance(A1, st.tdelta[1]);
+                step_advance(A1, tdelta[1]);
                 ci = w.cur[1];
                 di = c.dims[1];
             } else {
                 w.cur[2] += si;
-                step_advance(A2, st.tdelta[2]);
+                step_advance(A2, tdelta[2]);
                 ci = w.cur[2];
                 di = c.dims[2];
             }
@@ -982,7 +967,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
         sample_cell<MODE, CTF>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
         const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
         advance_position(w.P, c.vel, dtf, i, si);
-        const double td = i == 0 ? st.tdelta[0] : (i == 1 ? st.tdelta[1] : st.tdelta[2]);
+        const double td = i == 0 ? tdelta[0] : (i == 1 ? tdelta[1] : tdelta[2]);
         const double tn = dadd(tm, td);
         const long long Kn = dkey(tn);
         int ci, di;

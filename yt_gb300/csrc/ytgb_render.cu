@@ -14,15 +14,17 @@
 // _rn intrinsics (never contracted).  On GB300 the float64 pipe is far slower
 // than float32, so everything else is kept off it:
 //   * comparisons of walk values use order-preserving int64 keys;
-//   * per cell only `tmax += tdelta` and `exit_t - enter_t` run in float64;
+//   * per cell `tmax += tdelta` runs as an integer add on the bit pattern
+//     (float64 only when tmax leaves its binade) and `exit_t - enter_t` as
+//     an integer difference converted to float32 once;
 //   * the sample position is tracked in float32, in cell-local coordinates
 //     reset exactly on the axis the walk steps along;
 //   * bricks a ray clearly misses, faces it clearly does not enter through,
 //     and start points clearly outside a brick are rejected by float32 tests
 //     whose margins exceed their float32 error by orders of magnitude, before
 //     the exact float64 tests;
-//   * tdelta (a function of the ray and the brick's dds only) is reused
-//     across bricks of equal dds.
+//   * the per-walk state is kept small enough to stay in registers at 20
+//     warps per SM (tdelta is recomputed per walk rather than cached).
 // Sampling (trilinear, transfer function) runs in float32 on float32 brick
 // data.  The image accumulates as a float32 value plus a float32 error term
 // with error-free transformations (TwoSum, Knuth; TwoProduct via FMA), so
@@ -174,9 +176,9 @@ __device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, i
         }
     }
     if (a.counters) {
-        if (st.visits) atomicAdd(&sm.cnt[0], st.visits);
-        if (st.walks) atomicAdd(&sm.cnt[1], st.walks);
-        if (st.guarded) atomicAdd(&sm.cnt[3], st.guarded);
+        if (st.visits) atomicAdd(&sm.cnt[0], (unsigned long long)st.visits);
+        if (st.walks) atomicAdd(&sm.cnt[1], (unsigned long long)st.walks);
+        if (st.guarded) atomicAdd(&sm.cnt[3], (unsigned long long)st.guarded);
         if (active) atomicAdd(&sm.cnt[2], 1ull);
         __syncthreads();
         if (tid < 4 && sm.cnt[tid]) atomicAdd(a.counters + tid, sm.cnt[tid]);
