@@ -142,6 +142,12 @@ def test_direct_masks_match_host_pack(cuda):
     for k, (data, mask, le, re, dims) in enumerate(w.bricks):
         shape = tuple(int(d) for d in dims)
         m = np.ones(shape, np.uint8) if k % 3 else (rng.random(shape) < 0.8).astype(np.uint8)
+        if k % 4 == 1:
+            # a view starting off a 16-byte boundary
+            raw = np.empty(m.size + 7, np.uint8)
+            v = raw[k % 7 + 1: k % 7 + 1 + m.size].reshape(shape)
+            v[...] = m
+            m = v
         bricks.append((data, m, le, re, dims))
     a = BrickSet(bricks, device=cuda, direct=False)
     b = BrickSet(bricks, device=cuda, direct=True)

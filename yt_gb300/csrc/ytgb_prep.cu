@@ -105,7 +105,30 @@ gather_masks_kernel(const uint8_t *const *src, const int64_t *count, const int64
         const int64_t c = count[k];
         uint8_t *d = masks + dst_offset[k];
         int other = 0;
-        for (int64_t i = threadIdx.x; i < c; i += GATHER_BLOCK) {
+        // 16-byte reads over the link where the source allows (one request
+        // per warp moves 512 bytes instead of 32): the bytes before the first
+        // 16-byte boundary, the whole vectors, then the rest
+        const int64_t head = min(c, (int64_t)((16 - ((uintptr_t)s & 15)) & 15));
+        const int64_t nvec = (c - head) >> 4;
+        for (int64_t i = threadIdx.x; i < head; i += GATHER_BLOCK) {
+            const uint8_t v = s[i];
+            d[i] = v;
+            other |= v != 1;
+        }
+        const uint4 *sv = reinterpret_cast<const uint4 *>(s + head);
+        uint8_t *dv = d + head;
+        const bool dst16 = ((uintptr_t)dv & 15) == 0;
+        for (int64_t i = threadIdx.x; i < nvec; i += GATHER_BLOCK) {
+            const uint4 w = sv[i];
+            other |= (w.x != 0x01010101u) | (w.y != 0x01010101u) | (w.z != 0x01010101u) | (w.w != 0x01010101u);
+            if (dst16) {
+                reinterpret_cast<uint4 *>(dv)[i] = w;
+            } else {
+                const uint32_t wd[4] = {w.x, w.y, w.z, w.w};
+                for (int b = 0; b < 16; b++) dv[16 * i + b] = (uint8_t)(wd[b >> 2] >> (8 * (b & 3)));
+            }
+        }
+        for (int64_t i = head + (nvec << 4) + threadIdx.x; i < c; i += GATHER_BLOCK) {
             const uint8_t v = s[i];
             d[i] = v;
             other |= v != 1;
