@@ -193,11 +193,33 @@ def add_cells_to_image_offaxis(*, Xp, dXp, qty, weight, rotation, buffer, buffer
             raise ValueError("buffer and buffer_weight must be C-contiguous 2-d float64 arrays")
     dx_max = np.max(dXp)  # raises on no cells, as the reference does
     del dx_max
+    nx, ny = int(Nx), int(Ny)
+    if buffer.shape != (nx, ny) or buffer_weight.shape != (nx, ny):
+        raise ValueError(f"buffer and buffer_weight must have shape ({nx}, {ny})")
     splat = CellSplat(Xp, dXp, qty, weight, device=device)
-    lin, linw = splat.project(rotation, int(Nx), int(Ny), int(Npix_min))
-    host = torch.stack([lin, linw]).cpu().numpy()
-    buffer += _linear_to_image(host[0], int(Nx), int(Ny))
-    buffer_weight += _linear_to_image(host[1], int(Nx), int(Ny))
+    if nx != ny:
+        # pixel (i, j) lands at i * Nx + j of a linear buffer, read back with
+        # the reference's copy-back (Nx < Ny)
+        lin, linw = splat.project(rotation, nx, ny, int(Npix_min))
+        host = torch.stack([lin, linw]).cpu().numpy()
+        buffer += _linear_to_image(host[0], nx, ny)
+        buffer_weight += _linear_to_image(host[1], nx, ny)
+        return
+    # square images: the kernel accumulates straight into device copies of
+    # the caller's buffers (a buffer of zero bits, the usual new image, is
+    # cleared on the device instead of copied), which are then copied back
+    L = _lib.lib()
+    dev = splat.device
+    outs = []
+    for b in (buffer, buffer_weight):
+        flag = C.c_int32()
+        _lib.check(L.ytgb_host_prefault(b.ctypes.data, b.nbytes), "buffer prefault")
+        _lib.check(L.ytgb_host_is_uniform(b.ctypes.data, b.size, 0.0, 0, C.byref(flag)), "buffer check")
+        outs.append(torch.zeros(nx * ny, dtype=torch.float64, device=dev) if flag.value else
+                    torch.from_numpy(b).to(dev).reshape(-1))
+    splat.project(rotation, nx, ny, int(Npix_min), out=tuple(outs))
+    torch.from_numpy(buffer).copy_(outs[0].view(nx, ny))
+    torch.from_numpy(buffer_weight).copy_(outs[1].view(nx, ny))
 
 
 def project_cells(positions, dx, qty, center, width, rotation, resolution, weight=None, periodic=(True,) * 3,
