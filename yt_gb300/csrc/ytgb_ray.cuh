@@ -304,7 +304,7 @@ YTGB_HD void load_brick_f(const ytgb_brick *bp, BrickF &f) {
 // and walk_volume's 1e-10*dds face snapping).  True only when the ray misses
 // the grown box for every t in [0, max_t]; then no face test of walk_volume
 // can pass with intersect_t < max_t and the exact set-up returns 0.
-YTGB_HD bool surely_misses(const BrickF &b, const Ray &r, float max_t) {
+YTGB_HD bool surely_misses(const BrickF &b, const Ray &r, const float ifd[3], float max_t) {
     float t0 = -1e30f, t1 = 1e30f;
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
@@ -313,9 +313,8 @@ YTGB_HD bool surely_misses(const BrickF &b, const Ray &r, float max_t) {
         if (r.step[i] == 0) {
             if (r.fpos[i] < lo - m || r.fpos[i] > hi + m) return true;
         } else {
-            const float inv = 1.0f / r.fdir[i];
-            float ta = (lo - m - r.fpos[i]) * inv;
-            float tb = (hi + m - r.fpos[i]) * inv;
+            float ta = (lo - m - r.fpos[i]) * ifd[i];
+            float tb = (hi + m - r.fpos[i]) * ifd[i];
             if (ta > tb) {
                 const float tmp = ta;
                 ta = tb;
@@ -342,8 +341,8 @@ struct Walk {
 // decide comparisons whose outcome they prove (their margins exceed their
 // error bound by >= 80x), and the index and position of the entry point are
 // read from the bits of the float64 coordinate.
-YTGB_HD bool walk_setup(const BrickF &bf, const ytgb_brick *bp, const double *bounds, const Ray &r, double max_t,
-                        long long kmax, Walk &w) {
+YTGB_HD bool walk_setup(const BrickF &bf, const ytgb_brick *bp, const double *bounds, const Ray &r,
+                        const float ifd[3], double max_t, long long kmax, Walk &w) {
     double le[3], re[3], idds[3];
     YTGB_UNROLL
     for (int i = 0; i < 3; i++) {
@@ -373,20 +372,20 @@ YTGB_HD bool walk_setup(const BrickF &bf, const ytgb_brick *bp, const double *bo
             if (r.step[i] == 0) continue;
             const int x = (i + 1) % 3, y = (i + 2) % 3;
             // Float32 estimate of where the ray meets this face's plane.  The
-            // error of q is at most ~4 float32 roundings of
+            // error of q is at most ~6 float32 roundings of
             // (|e|+|p_i|)|d_x/d_i| + |tl d_x| + |p_x| (+ the edges' own
             // rounding); the margins are 1e-5 of that sum.  NaN or inf never
             // decides anything.
             const float e = r.step[i] > 0 ? bf.lef[i] : bf.ref[i];
             const float a0 = fabsf(e) + fabsf(r.fpos[i]);
-            const float tlf = (e - r.fpos[i]) / r.fdir[i];
+            const float tlf = (e - r.fpos[i]) * ifd[i];
             const float qx = r.fpos[x] + tlf * r.fdir[x];
             const float qy = r.fpos[y] + tlf * r.fdir[y];
-            const float sx = 1e-5f * (a0 * fabsf(r.fdir[x] / r.fdir[i]) + fabsf(tlf * r.fdir[x]) + fabsf(r.fpos[x]) +
+            const float sx = 1e-5f * (a0 * fabsf(r.fdir[x] * ifd[i]) + fabsf(tlf * r.fdir[x]) + fabsf(r.fpos[x]) +
                                       fabsf(bf.lef[x]) + fabsf(bf.ref[x]) + 1e-3f);
-            const float sy = 1e-5f * (a0 * fabsf(r.fdir[y] / r.fdir[i]) + fabsf(tlf * r.fdir[y]) + fabsf(r.fpos[y]) +
+            const float sy = 1e-5f * (a0 * fabsf(r.fdir[y] * ifd[i]) + fabsf(tlf * r.fdir[y]) + fabsf(r.fpos[y]) +
                                       fabsf(bf.lef[y]) + fabsf(bf.ref[y]) + 1e-3f);
-            const float st = 1e-5f * (a0 / fabsf(r.fdir[i]) + fabsf(tlf) + 1e-3f);
+            const float st = 1e-5f * (a0 * fabsf(ifd[i]) + fabsf(tlf) + 1e-3f);
             if (qx < bf.lef[x] - sx || qx > bf.ref[x] + sx || qy < bf.lef[y] - sy || qy > bf.ref[y] + sy || tlf < -st)
                 continue;  // clearly off the face: the exact test fails too
             const double tl = r.step[i] > 0 ? dmul(dsub(le[i], r.pos[i]), r.iv[i]) : dmul(dsub(re[i], r.pos[i]), r.iv[i]);
@@ -876,11 +875,17 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     const ytgb_brick *bp = a.bricks + bi;
     BrickF bf;
     load_brick_f(bp, bf);
-    if (surely_misses(bf, r, st.max_tf)) return;
+    // 1 / v_dir in float32 for the float32 pre-tests (a product with it is
+    // within two float32 roundings of the quotient; their margins are 1e-5
+    // and 1e-4 of the operands' scale)
+    float ifd[3];
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) ifd[i] = 1.0f / r.fdir[i];
+    if (surely_misses(bf, r, ifd, st.max_tf)) return;
     const double max_t = st.max_t;
     const long long kmax = dkey(st.max_t);
     Walk w;
-    if (!walk_setup(bf, bp, a.bounds, r, max_t, kmax, w)) return;
+    if (!walk_setup(bf, bp, a.bounds, r, ifd, max_t, kmax, w)) return;
     // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
     double tdelta[3];
     YTGB_UNROLL
