@@ -399,6 +399,17 @@ typedef struct ytgb_offaxis_args {
     int32_t pad;
 } ytgb_offaxis_args;
 
+/* The unnormalised stamps: for every level d in 1 .. max_depth-1 the depth
+ * zmax - zmin of the parallelepiped spanned by u, v, w from o at the centres
+ * of a min(2^d, nsx) x min(2^d, nsy) grid, and its hit mask
+ * (direct_integrate_cube, image_utilities.pyx:321-407, with
+ * check_in_parallelogram :296-318), written into stamp / mask (max_depth,
+ * nsx, nsy) zeroed by the caller; each level is then divided by its sum.
+ * Returns YTGB_ERR_INVALID where the reference raises ("This should not
+ * happen": a pixel met by one face). */
+int ytgb_offaxis_depths(const double *o, const double *u, const double *v, const double *w, int32_t nsx,
+                        int32_t nsy, int32_t max_depth, double *stamp, uint8_t *mask);
+
 /* Replaces add_cells_to_image_offaxis's cell loop (image_utilities.pyx:
  * 249-289): accumulates every cell into buffer / buffer_weight on the
  * device.  All pointers are device pointers; d_error (may be NULL) gets

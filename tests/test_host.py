@@ -338,3 +338,17 @@ def test_native_brick_layout_matches_numpy():
     assert np.array_equal(bounds, ref)
     assert np.array_equal(desc["bounds_offset"], starts[:-1].reshape(n, 3)[:, 0])
     assert (desc["mask_offset"] == -1).all()
+
+
+def test_native_offaxis_stamp_matches_numpy():
+    """ytgb_offaxis_depths (direct_integrate_cube natively) gives the numpy
+    restatement's stamps and masks bit for bit."""
+    from yt_gb300 import offaxis
+    from yt_gb300.camera import Camera
+
+    for pos, dxm, n in [((0.1, 0.3, -1.2), 0.05, 64), ((1.3, 0.2, 0.4), 0.2, 96), ((0.5, 0.5, -1.0), 0.02, 200),
+                        ((-0.4, 1.1, 0.3), 0.11, 48)]:
+        rot = Camera(pos, (0.5, 0.5, 0.5), (1, 1, 1), (n, n), lens_type="plane-parallel").inv_mat.T
+        s1, m1 = offaxis.offaxis_stamp(rot, dxm, n, n)
+        s2, m2 = offaxis.offaxis_stamp(rot, dxm, n, n, native=False)
+        assert np.array_equal(s1.view(np.int64), s2.view(np.int64)) and np.array_equal(m1, m2)

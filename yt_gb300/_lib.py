@@ -197,6 +197,7 @@ SIGNATURES = {
     "ytgb_octree_destroy": (None, [C.c_void_p]),
     "ytgb_render_octree": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ytgb_offaxis_cells": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ytgb_offaxis_depths": (C.c_int, [C.c_void_p] * 4 + [C.c_int32] * 3 + [C.c_void_p, C.c_void_p]),
     "ytgb_gather_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                      C.c_int64, C.c_void_p]),
     "ytgb_device_reads_host": (C.c_int, [C.c_void_p]),

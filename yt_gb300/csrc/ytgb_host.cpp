@@ -180,6 +180,67 @@ extern "C" int ytgb_brick_layout(int64_t n, const int64_t *dims, const double *l
     return YTGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Off-axis projection stamps: direct_integrate_cube (image_utilities.pyx:
+// 321-407) with check_in_parallelogram (:296-318), per stamp level.
+// ---------------------------------------------------------------------------
+static bool in_parallelogram(const double PA[2], const double PQ[3], const double PR[3], int sign, double nm[2]) {
+    const double det = PQ[0] * PR[1] - PQ[1] * PR[0];
+    if (det == 0) return false;
+    nm[0] = -(PA[0] * PQ[1] - PA[1] * PQ[0]) / det;
+    nm[1] = (PA[0] * PR[1] - PA[1] * PR[0]) / det;
+    const double s0 = sign * nm[0], s1 = sign * nm[1];
+    return 0 <= s0 && s0 <= 1 && 0 <= s1 && s1 <= 1;
+}
+
+extern "C" int ytgb_offaxis_depths(const double *o, const double *u, const double *v, const double *w, int32_t nsx,
+                                   int32_t nsy, int32_t max_depth, double *stamp, uint8_t *mask) {
+    if (!o || !u || !v || !w || !stamp || !mask || nsx < 1 || nsy < 1 || max_depth < 1 || max_depth > 30) {
+        ytgb_set_error("ytgb_offaxis_depths: bad arguments");
+        return YTGB_ERR_INVALID;
+    }
+    double ob[3];
+    for (int k = 0; k < 3; k++) ob[k] = o[k] + u[k] + v[k] + w[k];
+    for (int d = 1; d < max_depth; d++) {
+        const int sx = (1 << d) < nsx ? (1 << d) : nsx, sy = (1 << d) < nsy ? (1 << d) : nsy;
+        double *st = stamp + (int64_t)d * nsx * nsy;
+        uint8_t *mk = mask + (int64_t)d * nsx * nsy;
+        for (int i = 0; i < sx; i++) {
+            const double x0 = ((double)i + 0.5) * (1.0 / sx);
+            for (int j = 0; j < sy; j++) {
+                const double x1 = ((double)j + 0.5) * (1.0 / sy);
+                const double F[2] = {x0 - o[0], x1 - o[1]}, B[2] = {x0 - ob[0], x1 - ob[1]};
+                // the six faces in the reference's order: (point, PQ, PR, sign, z0, coefficient of nm[0], of nm[1])
+                struct Face {
+                    const double *pa, *pq, *pr;
+                    int sign;
+                    double z0, c0, c1;
+                } faces[6] = {{F, v, u, 1, o[2], u[2], v[2]},  {F, w, v, 1, o[2], v[2], w[2]},
+                              {F, w, u, 1, o[2], u[2], w[2]},  {B, v, u, -1, ob[2], u[2], v[2]},
+                              {B, w, v, -1, ob[2], v[2], w[2]}, {B, w, u, -1, ob[2], u[2], w[2]}};
+                double zmin = INFINITY, zmax = -INFINITY, nm[2];
+                int nhit = 0;
+                for (const Face &f : faces) {
+                    if (!in_parallelogram(f.pa, f.pq, f.pr, f.sign, nm)) continue;
+                    const double z = f.z0 + nm[0] * f.c0 + nm[1] * f.c1;
+                    if (z < zmin) zmin = z;
+                    if (z > zmax) zmax = z;
+                    nhit++;
+                }
+                if (nhit == 1) {
+                    ytgb_set_error("This should not happen");
+                    return YTGB_ERR_INVALID;
+                }
+                if (nhit > 1) {
+                    st[(int64_t)i * nsy + j] = zmax - zmin;
+                    mk[(int64_t)i * nsy + j] = 1;
+                }
+            }
+        }
+    }
+    return YTGB_OK;
+}
+
 extern "C" int ytgb_brick_rects(const ytgb_view *view, const ytgb_brick *bricks, int32_t n_bricks,
                                 const int32_t *order, int32_t n_order, int32_t *rects) {
     if (!view || !bricks || !rects || n_order < 0) {

@@ -69,11 +69,13 @@ def stamp_extent(dx_max, nx, ny, npix_min=4):
     return nsx, nsy, int(math.ceil(math.log2(max(nsx, nsy))))
 
 
-def offaxis_stamp(rotation, dx_max, nx, ny, npix_min=4):
+def offaxis_stamp(rotation, dx_max, nx, ny, npix_min=4, native=True):
     """The stamps and stamp masks of add_cells_to_image_offaxis
     (image_utilities.pyx:204-246): ``(max_depth, nsx, nsy)`` float64 and
     uint8 arrays; level 0 is the single 1, level d >= 1 the integrated cube
-    on min(2^d, nsx) x min(2^d, nsy) pixels, normalised to unit sum."""
+    on min(2^d, nsx) x min(2^d, nsy) pixels, normalised to unit sum.  The
+    depths come from ``ytgb_offaxis_depths`` (``native``) or from the numpy
+    restatement below; both give the same bits."""
     rotation = np.asarray(rotation, dtype=np.float64)
     center = np.array([0.5, 0.5, 0.5])
     w0 = 1 / np.sqrt(3.0)
@@ -84,14 +86,21 @@ def offaxis_stamp(rotation, dx_max, nx, ny, npix_min=4):
     nsx, nsy, max_depth = stamp_extent(dx_max, nx, ny, npix_min)
     stamp = np.zeros((max_depth, nsx, nsy), dtype=float)
     mask = np.zeros((max_depth, nsx, nsy), dtype=np.uint8)
-    for depth in range(max_depth):
-        if depth == 0:
-            stamp[0, 0, 0] = 1
-            continue
-        sx, sy = min(1 << depth, nsx), min(1 << depth, nsy)
-        buf, hit = _integrate_cube(o, a, b, c, sx, sy)
-        stamp[depth, :sx, :sy] += buf
-        mask[depth, :sx, :sy] = hit
+    stamp[0, 0, 0] = 1
+    if native:
+        # the per-pixel depths natively (the same float64 operations), the
+        # normalisation with numpy's own sum as the reference has it
+        vec = [np.ascontiguousarray(x, dtype=np.float64) for x in (o, a, b, c)]
+        st = _lib.lib().ytgb_offaxis_depths(*[x.ctypes.data for x in vec], nsx, nsy, max_depth, stamp.ctypes.data,
+                                            mask.ctypes.data)
+        if st != _lib.OK:
+            raise RuntimeError(_lib.lib().ytgb_last_error().decode(errors="replace"))
+    for depth in range(1, max_depth):
+        if not native:
+            sx, sy = min(1 << depth, nsx), min(1 << depth, nsy)
+            buf, hit = _integrate_cube(o, a, b, c, sx, sy)
+            stamp[depth, :sx, :sy] += buf
+            mask[depth, :sx, :sy] = hit
         stamp[depth] /= np.sum(stamp[depth])
     return stamp, mask
 
