@@ -18,6 +18,10 @@ namespace {
 using namespace ytgb;
 
 constexpr int OBLOCK = 128;
+// A block renders a 16 x 8 pixel tile, each warp an 8 x 4 sub-tile: rays
+// that traverse the octree together stay close on the image, so a warp's
+// lanes follow more of the same path than along a 32-pixel row.
+constexpr int OTILE_X = 16, OTILE_Y = 8;
 
 static_assert(sizeof(ytgb_onode) == sizeof(ONode), "ytgb_onode layout");
 
@@ -46,13 +50,16 @@ __global__ void __launch_bounds__(OBLOCK) octree_kernel(const ytgb_render_args a
     }
     __syncthreads();
     const ytgb_view &v = a.view;
-    const long long p = (long long)blockIdx.x * OBLOCK + tid;
-    const bool active = p < (long long)v.nx * v.ny;
+    const int tiles_y = (v.ny + OTILE_Y - 1) / OTILE_Y;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int vi = (int)(blockIdx.x / tiles_y) * OTILE_X + (warp & 1) * 8 + (lane & 7);
+    const int vj = (int)(blockIdx.x % tiles_y) * OTILE_Y + (warp >> 1) * 4 + (lane >> 3);
+    const bool active = vi < v.nx && vj < v.ny;
+    const long long p = (long long)vi * v.ny + vj;
     RayState st;
     double *img = active ? a.image + p * 4 : nullptr;
     ray_state_init(st, MODE != MODE_TRACE ? img : nullptr, 1.0, false, a.flags);
     if (active) {
-        const int vi = (int)(p / v.ny), vj = (int)(p % v.ny);
         Ray r;
         make_ray(v, vi, vj, r);
         OctreeView o;
@@ -160,8 +167,7 @@ int octree_launch(const ytgb_render_args *a, const ytgb_octree_args *o, size_t s
             return YTGB_ERR_CUDA;
         }
     }
-    const long long n = (long long)a->view.nx * a->view.ny;
-    const long long blocks = (n + OBLOCK - 1) / OBLOCK;
+    const long long blocks = (long long)((a->view.nx + OTILE_X - 1) / OTILE_X) * ((a->view.ny + OTILE_Y - 1) / OTILE_Y);
     if (blocks > 0x7fffffffll) {
         ytgb_set_error("ytgb_render_octree: image too large");
         return YTGB_ERR_INVALID;
