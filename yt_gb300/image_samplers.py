@@ -153,8 +153,7 @@ class ImageSampler:
 
     def cast_through_kdtree(self, pg, num_threads=0):
         """Record the brick; it is rendered at the next ``aimage`` read."""
-        data = list(pg.my_data)
-        if len(data) > 6:
+        if len(pg.my_data) > 6:
             raise ValueError("at most 6 fields per brick are supported")
         self._pending.append(pg)
         return 0
