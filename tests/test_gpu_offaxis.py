@@ -120,3 +120,26 @@ def test_project_cells_driver(cuda):
     assert img.shape == (64, 64, 2)
     close(img[..., 0], img[..., 1], 1e-14)
     assert img[32, 32, 0] > 0 and img[0, 0, 0] >= 0
+
+
+def test_offaxis_conserves_each_cells_total_at_full_size(cuda):
+    """Size-independent property at the benchmark's scale (217k cells of
+    levels 5-9, 1024^2): every cell's stamp sums to one, so a cell lying
+    inside the image deposits exactly q * dx^3 * Nx * Ny (and w * dx^3 Nx Ny
+    into the weight buffer); the image totals equal those sums."""
+    _, _, _, cells = testing.octree_cells(base_level=5, max_level=9, seed=0, percentile=85.0)
+    le, re = cells[:, 8:11], cells[:, 11:14]
+    # half the image width: every rotated cell stays inside the image
+    X = np.ascontiguousarray(((le + re) / 2 - 0.5) / 2)
+    dx = np.ascontiguousarray((re - le)[:, 0] / 2)
+    q = np.ascontiguousarray(cells[:, :8].mean(axis=1))
+    w = np.random.default_rng(1).uniform(0.5, 2.0, dx.size)
+    n = 1024
+    cam = Camera((0.05, 1.1, -0.16), (0.5, 0.5, 0.5), (1, 1, 1), (n, n), lens_type="plane-parallel")
+    b, bw = np.zeros((n, n)), np.zeros((n, n))
+    add_cells_to_image_offaxis(Xp=X, dXp=dx, qty=q, weight=w, rotation=np.ascontiguousarray(cam.inv_mat.T),
+                               buffer=b, buffer_weight=bw, Nx=n, Ny=n, device=cuda)
+    want_q = float(np.sum(q * dx ** 3) * n * n)
+    want_w = float(np.sum(w * dx ** 3) * n * n)
+    assert abs(b.sum() - want_q) <= 1e-10 * want_q
+    assert abs(bw.sum() - want_w) <= 1e-10 * want_w
