@@ -193,6 +193,8 @@ class BrickSet:
                 _lib.check(L.ytgb_pack_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, mk_brick.size,
                                              mbuf.data_ptr(), 0, C.byref(ones)), "ytgb_pack_masks")
                 desc["mask_offset"][mk_brick] = mdst
+        # (on the direct path the device sets the mask offsets of its copy;
+        # the host copy, used for the pixel rectangles, keeps -1)
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
         # the small tables first: copies from pageable memory wait for the
