@@ -821,6 +821,21 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
                 }
             }
             st.touched |= a.tf.grey_opacity == 1 ? 0xfu : 0x7u;
+        } else if (MODE == MODE_IPROJ) {
+            // InterpolatedProjectionSampler.sample (image_samplers.pyx:372-403):
+            // rgba[j] += v_j * dt for j < min(3, n_fields); the fields past
+            // the third are never read
+            const int n3 = c.nf < 3 ? c.nf : 3;
+            YTGB_UNROLL
+            for (int ch = 0; ch < 3; ch++) {
+                if (ch < n3) {
+                    const float v = trilinear(c.base + ch * c.fstride + off, c.sy, c.sx, fx, fy, fz);
+                    const float inc = fmul(v, dts);
+                    if (comp) acc_add(xh[ch], xl[ch], inc);
+                    else xh[ch] = fadd(xh[ch], inc);
+                    st.touched |= 1u << ch;
+                }
+            }
         } else {
             float dvs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             YTGB_UNROLL
