@@ -148,8 +148,11 @@ typedef struct ytgb_render_args {
     const double *bounds;      /* device cell-boundary tables (see ytgb_brick) */
     ytgb_tf tf;                /* by value, from ytgb_tf_pack (VR and light source) */
     const float *tf_tables;    /* device, VR and light source */
-    double *image;             /* device (nx,ny,4) float64, updated in place */
-    const double *zbuffer;     /* device (nx,ny) float64, or NULL (all ones) */
+    double *image;             /* device (nx,ny,4) float64, updated in place (or host
+                                * memory, where the device reads and writes pageable host
+                                * memory: see ytgb_device_reads_host) */
+    const double *zbuffer;     /* device (nx,ny) float64, or NULL (all ones); host memory
+                                * as for image */
     unsigned long long *counters; /* device [4]: cell visits, ray-brick walks, rays, cells
                                   * outside their brick (skipped); or NULL */
     int32_t *error;            /* device error word (0 = ok), or NULL */

@@ -68,8 +68,9 @@ def test_direct_gather_matches_host_pack(cuda, with_lo):
 
 
 def test_direct_sampler_matches_host_pack(cuda):
-    """The drop-in VolumeRenderSampler with device gather and direct
-    download against the host pack and staged download: identical images."""
+    """The drop-in VolumeRenderSampler with device gather and the render
+    written straight into the caller's host image, against the host pack
+    and staged download: identical images."""
     if not device_reads_host(cuda):
         pytest.skip("the device does not read pageable host memory")
     from yt_gb300.image_samplers import VolumeRenderSampler
@@ -93,12 +94,15 @@ def test_direct_sampler_matches_host_pack(cuda):
     assert np.array_equal(imgs[0].view(np.int64), imgs[1].view(np.int64))
 
 
-@pytest.mark.parametrize("case", ["image", "zbuffer", "both"])
-def test_sampler_rerenders_when_inputs_are_not_default(cuda, case):
-    """The drop-in sampler launches at once on a zero image and no zbuffer
-    and checks the caller's arrays meanwhile: an image that already holds
-    values (accumulation) or a zbuffer below 1 makes it render again on the
-    real inputs, matching the oracle's image and sample count."""
+@pytest.mark.parametrize("case", ["image", "zbuffer", "zbuffer-readonly", "both", "fortran", "fortran-zero"])
+@pytest.mark.parametrize("host_pack", ["0", "1"])
+def test_sampler_reads_inputs_that_are_not_default(cuda, case, host_pack):
+    """An image that already holds values (accumulation) or a zbuffer below
+    1 is read by the render: in place where the device reads host memory,
+    else uploaded for a second launch (the first assumed a zero image and
+    no zbuffer).  A Fortran-ordered image goes through a C-ordered copy.
+    A read-only zbuffer is read where it lies.  Each matches the oracle's
+    image and sample count."""
     from test_gpu_parity import oracle_render
     from yt_gb300 import _lib
     from yt_gb300.image_samplers import VolumeRenderSampler
@@ -110,20 +114,26 @@ def test_sampler_rerenders_when_inputs_are_not_default(cuda, case):
     rng = np.random.default_rng(9)
     nx, ny = p["image"].shape[:2]
     init = np.zeros((nx, ny, 4))
-    if case in ("image", "both"):
+    if case in ("image", "both", "fortran"):
         init = rng.uniform(0.0, 0.5, (nx, ny, 4))
     zb = np.ones((nx, ny))
-    if case in ("zbuffer", "both"):
+    if case in ("zbuffer", "zbuffer-readonly", "both"):
         zb = rng.uniform(0.2, 1.0, (nx, ny))
-    img = init.copy()
+    zb.flags.writeable = case != "zbuffer-readonly"
+    img = np.asfortranarray(init) if case.startswith("fortran") else init.copy()
+    os.environ["YTGB_HOST_PACK"] = host_pack
     s = VolumeRenderSampler(np.atleast_3d(p["vp_pos"]), np.atleast_3d(p["vp_dir"]), p["center"], p["bounds"], img,
                             p["x_vec"], p["y_vec"], p["width"], "KDTree", w.tf, 1, lens_type=p["lens_type"],
                             camera_data=p["camera_data"], zbuffer=zb)
-    for pg in w.kdtree.traverse(cam.viewpoint):
-        s(pg, num_threads=0)
-    out = s.aimage
+    try:
+        for pg in w.kdtree.traverse(cam.viewpoint):
+            s(pg, num_threads=0)
+        out = s.aimage
+    finally:
+        os.environ.pop("YTGB_HOST_PACK", None)
+    assert out is img
     ref, visits, _, _ = oracle_render(w.bricks, cam, w.order(cam), _lib.VOLUME_RENDER, tf=w.tf,
-                                      zbuffer=None if case == "image" else zb, image=init)
+                                      zbuffer=None if case in ("image", "fortran") else zb, image=init)
     assert relative_error(out, ref, channels=(0, 1, 2))[0] <= 1e-5
     assert int(s.last_counters[0]) == visits
 

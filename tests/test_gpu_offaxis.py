@@ -45,10 +45,15 @@ def octree_cells(base, top, seed):
     return (le + re) / 2, np.ascontiguousarray((re - le)[:, 0]), cells[:, :8].mean(axis=1)
 
 
-@pytest.mark.parametrize("res,pos", [((256, 256), (0.3, 0.8, -1.1)), ((200, 330), (1.4, -0.2, 0.6))])
-def test_offaxis_matches_oracle(cuda, res, pos):
+@pytest.mark.parametrize("res,pos,held", [((256, 256), (0.3, 0.8, -1.1), (1, 1)),
+                                          ((256, 256), (0.3, 0.8, -1.1), (0, 1)),
+                                          ((256, 256), (-0.9, 0.4, 0.2), (1, 0)),
+                                          ((200, 330), (1.4, -0.2, 0.6), (1, 1))])
+def test_offaxis_matches_oracle(cuda, res, pos, held):
     """A larger octree (levels 3-7): every stamp level from 16 to 64
-    subcells per row, accumulated into buffers that already hold values."""
+    subcells per row, accumulated into buffers that already hold values
+    (``held``: which of buffer and buffer_weight do; a zero buffer is the
+    launch the drop-in makes first, a held one makes it project again)."""
     ctr, dx, q = octree_cells(3, 7, 5)
     rng = np.random.default_rng(3)
     w = rng.uniform(0.5, 2.0, dx.size)
@@ -56,7 +61,7 @@ def test_offaxis_matches_oracle(cuda, res, pos):
     cam = Camera(pos, (0.5, 0.5, 0.5), (1, 1, 1), res, lens_type="plane-parallel")
     rot = np.ascontiguousarray(cam.inv_mat.T)
     X = np.ascontiguousarray(ctr - 0.5)
-    init = rng.uniform(0, 1, (2, nx, ny))
+    init = rng.uniform(0, 1, (2, nx, ny)) * np.asarray(held, dtype=np.float64)[:, None, None]
     b, bw = init[0].copy(), init[1].copy()
     add_cells_to_image_offaxis(Xp=X, dXp=dx, qty=q, weight=w, rotation=rot, buffer=b, buffer_weight=bw, Nx=nx,
                                Ny=ny, device=cuda)

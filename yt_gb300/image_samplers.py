@@ -28,7 +28,7 @@ import torch
 
 from . import _lib
 from . import transfer_functions as _tfm
-from .volume import BrickSet, brick_parts, render as _render
+from .volume import BrickSet, brick_parts, device_reads_host, render as _render
 
 
 def _device():
@@ -135,6 +135,7 @@ class ImageSampler:
         self.pdy = (self.bounds[3] - self.bounds[2]) / ny
         self.width = np.array(width, dtype=np.float64)
         self._pending = []
+        self._prefault = None
         self.n_samples = 1
         self.last_counters = None
         self.last_h2d_bytes = 0
@@ -155,8 +156,34 @@ class ImageSampler:
         """Record the brick; it is rendered at the next ``aimage`` read."""
         if len(pg.my_data) > 6:
             raise ValueError("at most 6 fields per brick are supported")
+        if not self._pending:
+            self._start_prefault()
         self._pending.append(pg)
         return 0
+
+    def _start_prefault(self):
+        """Fault the image's pages in for writing on a host thread while the
+        caller passes its bricks in, where the render will write the image in
+        place (flush() waits for it; a failure is left for flush() to meet
+        and report)."""
+        img = self._image
+        if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous
+                and img.flags.writeable and torch.cuda.is_available() and device_reads_host(_device())):
+            return
+        box = {"array": img, "ok": False}
+
+        def run():
+            box["start"] = time.perf_counter()
+            try:
+                _lib.check(_lib.lib().ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
+                box["ok"] = True
+            except BaseException:
+                pass
+            box["end"] = time.perf_counter()
+
+        box["thread"] = threading.Thread(target=run, daemon=True)
+        box["thread"].start()
+        self._prefault = box
 
     def cast_through_octree(self, pg, oct=None, num_threads=0):
         """ImageSampler.cast_through_octree (image_samplers.pyx:202-288): the
@@ -225,7 +252,11 @@ class ImageSampler:
         if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
             img = np.ascontiguousarray(img, dtype=np.float64)
         zb = np.ascontiguousarray(self.azbuffer, dtype=np.float64)
-        # The render is launched on the usual inputs -- a new image (all zero
+        if device_reads_host(dev):
+            self._flush_in_place(pending, dev, L, img, zb, t0)
+            return
+        # Otherwise (a device that reaches host memory only through copies)
+        # the render is launched on the usual inputs -- a new image (all zero
         # bits) and a zbuffer of ones, which clips nothing
         # (image_samplers.pyx:185, max_t = 1) -- while a host thread checks
         # that they are: it faults the image's pages in for writing (so that
@@ -246,9 +277,7 @@ class ImageSampler:
             except BaseException as e:  # re-raised on the calling thread
                 checks["error"] = e
 
-        # (with the device gather in flight: pending keeps the bricks alive
-        # and the stream is synchronised below before they may change)
-        bricks = BrickSet(pending, device=dev, with_lo=self._with_lo, sync=False)
+        bricks = BrickSet(pending, device=dev, with_lo=self._with_lo, direct=False)
         t1 = time.perf_counter()
         order = np.arange(len(pending), dtype=np.int32)
         # the pixel rectangles on all cores before the checks take them
@@ -259,12 +288,8 @@ class ImageSampler:
         px_pos = px_dir = None
         h2d = 0
         if self._px_pos is not None:
-            if bricks.direct:
-                # the kernel reads each pixel's ray from the host arrays
-                px_pos, px_dir = self._px_pos, self._px_dir
-            else:
-                px_pos = torch.from_numpy(self._px_pos).to(dev)
-                px_dir = torch.from_numpy(self._px_dir).to(dev)
+            px_pos = torch.from_numpy(self._px_pos).to(dev)
+            px_dir = torch.from_numpy(self._px_dir).to(dev)
             h2d += self._px_pos.nbytes + self._px_dir.nbytes
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -296,17 +321,12 @@ class ImageSampler:
         _lib.check(L.ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
         keep.clear()
         t3 = time.perf_counter()
-        if bricks.direct:
-            # a device that reads and writes pageable host memory copies
-            # straight into the caller's (prefaulted) array at link speed
-            torch.from_numpy(img).copy_(image_d)
-        else:
-            # device -> pinned staging (full link speed), then into the
-            # caller's array on all host cores
-            with _stage["lock"]:
-                stage = _staging(img.nbytes)[: img.size].view(image_d.shape)
-                stage.copy_(image_d)
-                _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
+        # device -> pinned staging (full link speed), then into the caller's
+        # array on all host cores
+        with _stage["lock"]:
+            stage = _staging(img.nbytes)[: img.size].view(image_d.shape)
+            stage.copy_(image_d)
+            _lib.check(L.ytgb_host_copy(img.ctypes.data, stage.data_ptr(), img.nbytes, 0), "image copy")
         if img is not self._image:
             self._image[...] = img
         self.last_counters = counters.cpu().numpy()
@@ -321,6 +341,59 @@ class ImageSampler:
         # download: the image into the caller's array
         self.last_timings = {"pack_ms": 1e3 * (t1 - t0), "launch_ms": 1e3 * (t2 - t1), "render_ms": 1e3 * (t3 - t2),
                              "download_ms": 1e3 * (t4 - t3)}
+
+    def _flush_in_place(self, pending, dev, L, img, zb, t0):
+        """flush() on a device that reads and writes pageable host memory:
+        the kernel accumulates straight into the caller's image and reads
+        the zbuffer where they lie, so nothing is copied back.  The image's
+        pages are faulted in for writing from the first brick on, on a host
+        thread (the device would otherwise fault on each page); flush()
+        waits for that once the bricks are gathered.  As with yt's sampler,
+        a render that fails (an error word raised below) may have written
+        part of the image."""
+        pre, self._prefault = self._prefault, None
+        # (the device gather runs while the rectangles are computed: pending
+        # keeps the bricks alive and the stream is synchronised below before
+        # they may change)
+        bricks = BrickSet(pending, device=dev, with_lo=self._with_lo, direct=True, sync=False)
+        order = np.arange(len(pending), dtype=np.int32)
+        rects = bricks.rects(self._view, order)
+        t_bricks = time.perf_counter()
+        if pre is not None:
+            pre["thread"].join()
+        if pre is None or pre["array"] is not img or not pre["ok"]:
+            _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
+        t1 = time.perf_counter()
+        counters = torch.zeros(4, dtype=torch.int64, device=dev)
+        error = torch.zeros(1, dtype=torch.int32, device=dev)
+        stream = torch.cuda.current_stream(dev)
+        keep = []
+        _render(bricks, self._view, order, self.kind, img, tf=self._tf(), zbuffer=zb, n_samples=self.n_samples,
+                flags=self.flags, counters=counters, error=error, px_pos=self._px_pos, px_dir=self._px_dir,
+                light=self._light(), keep=keep, rects=rects)
+        t2 = time.perf_counter()
+        _lib.check(L.ytgb_check_error(error.data_ptr(), stream.cuda_stream), "render")
+        keep.clear()
+        t3 = time.perf_counter()
+        if img is not self._image:
+            self._image[...] = img
+        self.last_counters = counters.cpu().numpy()
+        t4 = time.perf_counter()
+        # bytes the device read from host memory (bricks, boundary tables,
+        # descriptors, masks, order and rectangles, per-pixel rays, image
+        # and zbuffer) and wrote to it (image, counters)
+        h2d = img.nbytes + zb.nbytes
+        if self._px_pos is not None:
+            h2d += self._px_pos.nbytes + self._px_dir.nbytes
+        self.last_h2d_bytes = int(bricks.upload_bytes + h2d + 20 * len(pending))
+        self.last_d2h_bytes = int(img.nbytes + 4 * 8)
+        # pack: bricks gathered and rectangles computed (bricks_at), image
+        # pages faulted in; launch; render: until the image is written;
+        # download: the counters
+        self.last_timings = {"pack_ms": 1e3 * (t1 - t0), "launch_ms": 1e3 * (t2 - t1), "render_ms": 1e3 * (t3 - t2),
+                             "download_ms": 1e3 * (t4 - t3), "bricks_at_ms": 1e3 * (t_bricks - t0)}
+        if pre is not None and "end" in pre:
+            self.last_timings.update(prefault_from_ms=1e3 * (pre["start"] - t0), prefault_ms=1e3 * (pre["end"] - pre["start"]))
 
     def ensure_code_unit_params(self, params):
         for name in ["center", "vp_pos", "vp_dir", "width"]:

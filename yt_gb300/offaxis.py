@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 
 import numpy as np
 import torch
@@ -215,18 +216,37 @@ def add_cells_to_image_offaxis(*, Xp, dXp, qty, weight, rotation, buffer, buffer
         buffer_weight += _linear_to_image(host[1], nx, ny)
         return
     # square images: the kernel accumulates straight into device copies of
-    # the caller's buffers (a buffer of zero bits, the usual new image, is
-    # cleared on the device instead of copied), which are then copied back
+    # the caller's buffers, which are then copied back.  The projection is
+    # launched on buffers of zero bits (the usual new image) while a host
+    # thread faults the buffers' pages in and checks that they are zero;
+    # otherwise they are uploaded and the projection is run again.
     L = _lib.lib()
     dev = splat.device
-    outs = []
-    for b in (buffer, buffer_weight):
-        flag = C.c_int32()
-        _lib.check(L.ytgb_host_prefault(b.ctypes.data, b.nbytes), "buffer prefault")
-        _lib.check(L.ytgb_host_is_uniform(b.ctypes.data, b.size, 0.0, 0, C.byref(flag)), "buffer check")
-        outs.append(torch.zeros(nx * ny, dtype=torch.float64, device=dev) if flag.value else
-                    torch.from_numpy(b).to(dev).reshape(-1))
-    splat.project(rotation, nx, ny, int(Npix_min), out=tuple(outs))
+    checks = {}
+
+    def host_checks():
+        try:
+            for b in (buffer, buffer_weight):
+                flag = C.c_int32()
+                _lib.check(L.ytgb_host_prefault(b.ctypes.data, b.nbytes), "buffer prefault")
+                _lib.check(L.ytgb_host_is_uniform(b.ctypes.data, b.size, 0.0, 0, C.byref(flag)), "buffer check")
+                checks[id(b)] = bool(flag.value)
+        except BaseException as e:  # re-raised on the calling thread
+            checks["error"] = e
+
+    outs = tuple(torch.zeros(nx * ny, dtype=torch.float64, device=dev) for _ in range(2))
+    checker = threading.Thread(target=host_checks, daemon=True)
+    checker.start()
+    try:
+        splat.project(rotation, nx, ny, int(Npix_min), out=outs)
+    finally:
+        checker.join()
+    if "error" in checks:
+        raise checks["error"]
+    if not (checks[id(buffer)] and checks[id(buffer_weight)]):
+        outs = tuple(torch.zeros(nx * ny, dtype=torch.float64, device=dev) if checks[id(b)] else
+                     torch.from_numpy(b).to(dev).reshape(-1) for b in (buffer, buffer_weight))
+        splat.project(rotation, nx, ny, int(Npix_min), out=outs)
     torch.from_numpy(buffer).copy_(outs[0].view(nx, ny))
     torch.from_numpy(buffer_weight).copy_(outs[1].view(nx, ny))
 

@@ -378,7 +378,19 @@ def set_light(args, bricks, light):
 
 
 def _ptr(t):
-    return None if t is None else t.data_ptr()
+    if t is None:
+        return None
+    return t.ctypes.data if isinstance(t, np.ndarray) else t.data_ptr()
+
+
+def _f64_contiguous(t, writeable=False) -> bool:
+    if isinstance(t, np.ndarray):
+        return t.dtype == np.float64 and t.flags.c_contiguous and (t.flags.writeable or not writeable)
+    return t.dtype == torch.float64 and t.is_contiguous()
+
+
+def _numel(t) -> int:
+    return t.size if isinstance(t, np.ndarray) else t.numel()
 
 
 def check_inputs(bricks: BrickSet, view: _lib.View, order, kind, image=None, zbuffer=None, px_pos=None,
@@ -396,12 +408,14 @@ def check_inputs(bricks: BrickSet, view: _lib.View, order, kind, image=None, zbu
         k = int(short[0])
         raise ValueError(f"brick {k} has {bricks.min_elems[k]} values per field; this sampler reads {need[k]}")
     nx, ny = view.nx, view.ny
-    if image is not None and tuple(image.shape) != (nx, ny, 4) or (image is not None and (
-            image.dtype != torch.float64 or not image.is_contiguous())):
-        raise ValueError(f"image must be a contiguous float64 ({nx}, {ny}, 4) tensor")
-    if zbuffer is not None and (zbuffer.numel() != nx * ny or zbuffer.dtype != torch.float64
-                                or not zbuffer.is_contiguous()):
-        raise ValueError("zbuffer must be a contiguous float64 (nx, ny) tensor")
+    for t in (image, zbuffer):
+        # host arrays: only where the device reads and writes them in place
+        if isinstance(t, np.ndarray) and not device_reads_host(bricks.device):
+            raise ValueError("host image and zbuffer arrays need a device that reads pageable host memory")
+    if image is not None and tuple(image.shape) != (nx, ny, 4) or (image is not None and not _f64_contiguous(image, True)):
+        raise ValueError(f"image must be a contiguous float64 ({nx}, {ny}, 4) tensor or array")
+    if zbuffer is not None and (_numel(zbuffer) != nx * ny or not _f64_contiguous(zbuffer)):
+        raise ValueError("zbuffer must be a contiguous float64 (nx, ny) tensor or array")
     if view.lens == _lib.LENS_PER_PIXEL:
         for t in (px_pos, px_dir):
             if isinstance(t, np.ndarray):
@@ -420,7 +434,9 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
            stream: torch.cuda.Stream | None = None, rects: np.ndarray | None = None,
            keep: list | None = None, light=None) -> None:
     """Launch ytgb_render for one view.  ``image`` is a (nx, ny, 4) float64
-    device tensor updated in place; ``tf`` a PackedTF for volume rendering.
+    device tensor updated in place -- or, on a device that reads and writes
+    pageable host memory, a host array (likewise ``zbuffer``); ``tf`` a
+    PackedTF for volume rendering.
     Device temporaries that must outlive the asynchronous launch are appended
     to ``keep`` when given."""
     dev = bricks.device
@@ -454,7 +470,7 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
     if tf is not None:
         args.tf = tf.header
         args.tf_tables = tf.device_tables(dev).data_ptr()
-    args.image = image.data_ptr()
+    args.image = _ptr(image)
     args.zbuffer = _ptr(zbuffer)
     if kind == _lib.LIGHT_SOURCE:
         set_light(args, bricks, light)
