@@ -141,13 +141,19 @@ class ImageSampler:
         self.last_h2d_bytes = 0
         self.last_d2h_bytes = 0
         self.last_timings = {}
+        if volume_method == "KDTree":
+            self._start_prefault()
 
     # ---- the call surface ---------------------------------------------------
-    def __call__(self, pg, **kwa):
+    def __call__(self, pg, num_threads=0, **kwa):
         if self.volume_method == "KDTree":
-            return self.cast_through_kdtree(pg, **kwa)
+            # cast_through_kdtree, inlined: yt makes one call per brick
+            if len(pg.my_data) > 6:
+                raise ValueError("at most 6 fields per brick are supported")
+            self._pending.append(pg)
+            return 0
         elif self.volume_method == "Octree":
-            return self.cast_through_octree(pg, **kwa)
+            return self.cast_through_octree(pg, num_threads=num_threads, **kwa)
         else:
             raise NotImplementedError(
                 f'Volume rendering has not been implemented for method: "{self.volume_method}"')
@@ -156,16 +162,14 @@ class ImageSampler:
         """Record the brick; it is rendered at the next ``aimage`` read."""
         if len(pg.my_data) > 6:
             raise ValueError("at most 6 fields per brick are supported")
-        if not self._pending:
-            self._start_prefault()
         self._pending.append(pg)
         return 0
 
     def _start_prefault(self):
         """Fault the image's pages in for writing on a host thread while the
         caller passes its bricks in, where the render will write the image in
-        place (flush() waits for it; a failure is left for flush() to meet
-        and report)."""
+        place (the first flush() waits for it and faults in any image it was
+        not given; a failure is left for flush() to meet and report)."""
         img = self._image
         if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous
                 and img.flags.writeable and torch.cuda.is_available() and device_reads_host(_device())):
