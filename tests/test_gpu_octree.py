@@ -62,9 +62,14 @@ def test_octree_matches_oracle(cuda, kind):
     assert np.array_equal(c, cr) and np.array_equal(h, hr)
 
 
-def test_octree_drop_in(cuda):
+@pytest.mark.parametrize("held", [False, True])
+@pytest.mark.parametrize("host_pack", ["0", "1"])
+def test_octree_drop_in(cuda, held, host_pack, monkeypatch):
     """VolumeRenderSampler(..., "Octree") called as OctreeVolumeSource.render
-    calls it: sampler(pg, oct=octree) with the 14-values-per-cell grid."""
+    calls it: sampler(pg, oct=octree) with the 14-values-per-cell grid,
+    into a new image or one that holds values; rendered in the caller's host
+    arrays where the device reads host memory, else through device copies
+    (YTGB_HOST_PACK=1)."""
     from yt_gb300.image_samplers import VolumeRenderSampler
     from yt_gb300.partitioned_grid import PartitionedGrid
 
@@ -74,11 +79,15 @@ def test_octree_drop_in(cuda):
     le, re = np.zeros(3), np.ones(3)
     dt = cells.reshape(1, -1, 14, 1)
     pg = PartitionedGrid(0, dt, np.ones(dt.shape[1:], dtype=np.uint8), le, re, np.array([1, 1, 1]), n_fields=1)
+    monkeypatch.setenv("YTGB_HOST_PACK", host_pack)
+    init = np.random.default_rng(2).uniform(0.0, 0.3, p["image"].shape) if held else np.zeros(p["image"].shape)
+    p["image"][...] = init
     s = VolumeRenderSampler(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"], p["x_vec"], p["y_vec"],
                             p["width"], "Octree", tf, 2, lens_type=p["lens_type"], camera_data=p["camera_data"])
     s(pg, oct=oc)
     img = s.aimage.copy()
     p2 = cam.sampler_params()
+    p2["image"][...] = init
     so = ocpu.OracleSampler("volume_render", p2["vp_pos"], p2["vp_dir"], p2["center"], p2["bounds"], p2["image"],
                             p2["x_vec"], p2["y_vec"], p2["width"], lens_type=p2["lens_type"],
                             camera_data=p2["camera_data"], n_samples=2, tf=tf)

@@ -82,8 +82,8 @@ def make_view(vp_pos, vp_dir, center, bounds, nx, ny, x_vec, y_vec, width, lens_
             v.extent = _lib.EXTENT_PERSPECTIVE
         else:
             v.extent = _lib.EXTENT_NULL
-        px_pos = np.ascontiguousarray(vp_pos.reshape(nx, ny, 3))
-        px_dir = np.ascontiguousarray(vp_dir.reshape(nx, ny, 3))
+        px_pos = np.ascontiguousarray(np.asarray(vp_pos).reshape(nx, ny, 3), dtype=np.float64)
+        px_dir = np.ascontiguousarray(np.asarray(vp_dir).reshape(nx, ny, 3), dtype=np.float64)
     for i in range(3):
         v.center[i] = float(center[i])
         v.x_vec[i] = float(x_vec[i])
@@ -141,8 +141,7 @@ class ImageSampler:
         self.last_h2d_bytes = 0
         self.last_d2h_bytes = 0
         self.last_timings = {}
-        if volume_method == "KDTree":
-            self._start_prefault()
+        self._start_prefault()
 
     # ---- the call surface ---------------------------------------------------
     def __call__(self, pg, num_threads=0, **kwa):
@@ -164,6 +163,17 @@ class ImageSampler:
             raise ValueError("at most 6 fields per brick are supported")
         self._pending.append(pg)
         return 0
+
+    def _await_prefault(self, img, L):
+        """Wait for the prefault _start_prefault began, or fault ``img``'s
+        pages in now if it was not that array or did not succeed.  Returns
+        the prefault's record (or None)."""
+        pre, self._prefault = self._prefault, None
+        if pre is not None:
+            pre["thread"].join()
+        if pre is None or pre["array"] is not img or not pre["ok"]:
+            _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
+        return pre
 
     def _start_prefault(self):
         """Fault the image's pages in for writing on a host thread while the
@@ -208,20 +218,33 @@ class ImageSampler:
         img = self._image
         if not (isinstance(img, np.ndarray) and img.dtype == np.float64 and img.flags.c_contiguous):
             img = np.ascontiguousarray(img, dtype=np.float64)
-        image_d = torch.from_numpy(img).to(dev)
-        px_pos = torch.from_numpy(self._px_pos).to(dev)
-        px_dir = torch.from_numpy(self._px_dir).to(dev)
         view = self._view
-        view.px_pos, view.px_dir = px_pos.data_ptr(), px_dir.data_ptr()
+        in_place = device_reads_host(dev)
+        if in_place:
+            # the kernel reads the rays and accumulates into the image where
+            # they lie (as flush() does)
+            self._await_prefault(img, _lib.lib())
+            image_d = img
+            view.px_pos, view.px_dir = self._px_pos.ctypes.data, self._px_dir.ctypes.data
+        else:
+            image_d = torch.from_numpy(img).to(dev)
+            px_pos = torch.from_numpy(self._px_pos).to(dev)
+            px_dir = torch.from_numpy(self._px_dir).to(dev)
+            view.px_pos, view.px_dir = px_pos.data_ptr(), px_dir.data_ptr()
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)
-        render_octree(vol, view, self.kind, image_d, tf=self._tf(), n_samples=self.n_samples, flags=self.flags,
-                      counters=counters, error=error, light=self._light())
-        stream = torch.cuda.current_stream(dev)
-        _lib.check(_lib.lib().ytgb_check_error(error.data_ptr(), stream.cuda_stream), "octree render")
-        self._image[...] = image_d.cpu().numpy()
+        try:
+            render_octree(vol, view, self.kind, image_d, tf=self._tf(), n_samples=self.n_samples, flags=self.flags,
+                          counters=counters, error=error, light=self._light())
+            stream = torch.cuda.current_stream(dev)
+            _lib.check(_lib.lib().ytgb_check_error(error.data_ptr(), stream.cuda_stream), "octree render")
+        finally:
+            view.px_pos = view.px_dir = None
+        if not in_place:
+            self._image[...] = image_d.cpu().numpy()
+        elif img is not self._image:
+            self._image[...] = img
         self.last_counters = counters.cpu().numpy()
-        view.px_pos = view.px_dir = None
         return 0
 
     @property
@@ -355,7 +378,6 @@ class ImageSampler:
         waits for that once the bricks are gathered.  As with yt's sampler,
         a render that fails (an error word raised below) may have written
         part of the image."""
-        pre, self._prefault = self._prefault, None
         # (the device gather runs while the rectangles are computed: pending
         # keeps the bricks alive and the stream is synchronised below before
         # they may change)
@@ -363,10 +385,7 @@ class ImageSampler:
         order = np.arange(len(pending), dtype=np.int32)
         rects = bricks.rects(self._view, order)
         t_bricks = time.perf_counter()
-        if pre is not None:
-            pre["thread"].join()
-        if pre is None or pre["array"] is not img or not pre["ok"]:
-            _lib.check(L.ytgb_host_prefault(img.ctypes.data, img.nbytes), "image prefault")
+        pre = self._await_prefault(img, L)
         t1 = time.perf_counter()
         counters = torch.zeros(4, dtype=torch.int64, device=dev)
         error = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -123,11 +123,14 @@ class OctreeVolume:
 def render_octree(vol: OctreeVolume, view: _lib.View, kind: int, image: torch.Tensor, tf=None, n_samples=1,
                   flags=0, counters=None, error=None, light=None, stream=None):
     """One ``ytgb_render_octree`` launch into ``image`` ((nx, ny, 4) float64
-    device tensor, updated in place)."""
-    from .volume import _ptr, normalised_light
+    device tensor, updated in place -- or a host array, on a device that
+    reads and writes pageable host memory)."""
+    from .volume import _f64_contiguous, _ptr, device_reads_host, normalised_light
 
-    if tuple(image.shape) != (view.nx, view.ny, 4) or image.dtype != torch.float64 or not image.is_contiguous():
-        raise ValueError(f"image must be a contiguous float64 ({view.nx}, {view.ny}, 4) tensor")
+    if isinstance(image, np.ndarray) and not device_reads_host(vol.device):
+        raise ValueError("a host image needs a device that reads pageable host memory")
+    if tuple(image.shape) != (view.nx, view.ny, 4) or not _f64_contiguous(image, True):
+        raise ValueError(f"image must be a contiguous float64 ({view.nx}, {view.ny}, 4) tensor or array")
     a = _lib.RenderArgs()
     a.kind = int(kind)
     a.n_samples = int(n_samples)
@@ -137,7 +140,7 @@ def render_octree(vol: OctreeVolume, view: _lib.View, kind: int, image: torch.Te
     if tf is not None:
         a.tf = tf.header
         a.tf_tables = tf.device_tables(vol.device).data_ptr()
-    a.image = image.data_ptr()
+    a.image = _ptr(image)
     a.counters = _ptr(counters)
     a.error = _ptr(error)
     if kind == _lib.LIGHT_SOURCE:
