@@ -181,7 +181,8 @@ def test_direct_masks_match_host_pack(cuda):
 def test_render_with_resident_tables(cuda):
     """render(..., tables=render_tables(...)) -- the rectangles and order kept
     on the device across launches -- gives the same image, bit for bit, as
-    the per-launch upload, and a table of the wrong size is rejected."""
+    the per-launch upload, and a table made for another order is
+    rejected."""
     from yt_gb300 import _lib
     from yt_gb300.render import Renderer
     from yt_gb300.volume import render, render_tables
@@ -207,4 +208,4 @@ def test_render_with_resident_tables(cuda):
         assert np.array_equal(imgs[0].view(np.int64), x.view(np.int64))
     with pytest.raises(ValueError):
         render(r.bricks, view, order, _lib.VOLUME_RENDER, torch.zeros((nx, ny, 4), dtype=torch.float64, device=cuda),
-               tf=r.packed, px_pos=px_pos, px_dir=px_dir, tables=tables[:-1])
+               tf=r.packed, px_pos=px_pos, px_dir=px_dir, tables=render_tables(r.bricks, view, order[::-1]))

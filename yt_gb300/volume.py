@@ -434,17 +434,29 @@ def _table(rects: np.ndarray, order: np.ndarray) -> np.ndarray:
     return tab
 
 
-def render_tables(bricks: BrickSet, view: _lib.View, order: np.ndarray, rects: np.ndarray | None = None
-                  ) -> torch.Tensor:
+class RenderTables:
     """The table one render reads -- each order entry's pixel rectangle (4
-    int32), then the order -- on the device, for ``render(..., tables=)``
-    to keep resident across launches of the same view and order."""
+    int32), then the order -- on the device, with the host copy of the
+    order it was made for (the kernel indexes the bricks by the device
+    copy, so render() accepts it only for that same order)."""
+
+    def __init__(self, table: torch.Tensor, order: np.ndarray):
+        self.table = table
+        self.order = order.copy()
+
+
+def render_tables(bricks: BrickSet, view: _lib.View, order: np.ndarray, rects: np.ndarray | None = None
+                  ) -> RenderTables:
+    """A :class:`RenderTables` for ``render(..., tables=)``, to keep resident
+    across launches of the same view and order."""
     order = np.ascontiguousarray(order, dtype=np.int32)
+    if order.size and (order.min() < 0 or order.max() >= bricks.n):
+        raise ValueError("order entry out of range")
     if rects is None:
         rects = bricks.rects(view, order)
     if np.shape(rects) != (order.size, 4):
         raise ValueError("rects must hold 4 entries per order entry")
-    return torch.from_numpy(_table(rects, order)).to(bricks.device)
+    return RenderTables(torch.from_numpy(_table(rects, order)).to(bricks.device), order)
 
 
 def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, image: torch.Tensor,
@@ -452,7 +464,7 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
            counters: torch.Tensor | None = None, error: torch.Tensor | None = None,
            px_pos: torch.Tensor | None = None, px_dir: torch.Tensor | None = None,
            stream: torch.cuda.Stream | None = None, rects: np.ndarray | None = None,
-           keep: list | None = None, light=None, tables: torch.Tensor | None = None) -> None:
+           keep: list | None = None, light=None, tables: RenderTables | None = None) -> None:
     """Launch ytgb_render for one view.  ``image`` is a (nx, ny, 4) float64
     device tensor updated in place -- or, on a device that reads and writes
     pageable host memory, a host array (likewise ``zbuffer``); ``tf`` a
@@ -472,11 +484,11 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
         with torch.cuda.stream(stream):
             tab_d = torch.from_numpy(_table(rects, order)).pin_memory().to(dev, non_blocking=True)
     else:
-        if (tables.dtype != torch.int32 or tables.numel() != order.size * 5 or not tables.is_contiguous()
-                or tables.device.type != "cuda" or (dev.index is not None and tables.device.index != dev.index)):
-            raise ValueError(f"tables must be the contiguous int32 device tensor of render_tables "
-                             f"({order.size * 5} entries on {dev})")
-        tab_d = tables
+        t = tables.table if isinstance(tables, RenderTables) else None
+        if (t is None or not np.array_equal(tables.order, order) or t.device.type != "cuda"
+                or (dev.index is not None and t.device.index != dev.index)):
+            raise ValueError(f"tables must come from render_tables for this order, on {dev}")
+        tab_d = t
     args = _lib.RenderArgs()
     args.kind = int(kind)
     args.n_samples = int(n_samples)
