@@ -233,12 +233,21 @@ int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind
  * static device region of this library that also holds the work-queue
  * counter, then the persistent launch runs from there.  No counterpart in
  * the reference (yt renders one camera at a time and allocates per call).
+ * The host table is checked against the arguments before anything is
+ * queued (each entry's arguments, sampler kind and table layout, smem_bytes
+ * against the entries' tables, the tile numbering ytgb_batch_plan writes for
+ * tile_shape, total_tiles); a mismatch returns YTGB_ERR_INVALID.
  * Limits: at most YTGB_NOALLOC_MAX_ENTRIES views per call (more is rejected
  * with YTGB_ERR_INVALID); the region is per device, so calls on one device
  * must not overlap in time (use one stream, or wait for the previous call's
  * work); the first call on a device looks the region up
- * (cudaGetSymbolAddress) -- make it outside any stream capture.  The
- * counter is cleared by every call; nothing needs to be zero beforehand. */
+ * (cudaGetSymbolAddress) -- make it outside any stream capture -- and keeps
+ * the address for the life of the process, so do not call it again on a
+ * device after cudaDeviceReset.  h_entries in pageable memory may be reused
+ * once the call returns; in page-locked memory (cudaHostAlloc,
+ * cudaHostRegister) it is read asynchronously and must stay unchanged until
+ * the stream has passed the call.  The counter is cleared by every call;
+ * nothing needs to be zero beforehand. */
 #define YTGB_NOALLOC_MAX_ENTRIES 128
 int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind, int32_t ctf_fast,
                               int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t blocks,

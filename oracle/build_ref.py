@@ -43,7 +43,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 GEN = OUT / "gen"
-REF_ROOT = Path(os.environ.get("YTGB_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: YTGB_REFERENCE_ROOT, else a directory named
+# "reference" beside this checkout
+REF_ROOT = Path(os.environ.get("YTGB_REFERENCE_ROOT", str(HERE.parent.parent / "reference")))
 LIB_REL = Path("yt/utilities/lib")
 
 MODULES = [

@@ -209,3 +209,13 @@ def test_render_with_resident_tables(cuda):
     with pytest.raises(ValueError):
         render(r.bricks, view, order, _lib.VOLUME_RENDER, torch.zeros((nx, ny, 4), dtype=torch.float64, device=cuda),
                tf=r.packed, px_pos=px_pos, px_dir=px_dir, tables=render_tables(r.bricks, view, order[::-1]))
+    # a narrower field of view keeps the kd order (same viewpoint) but not
+    # the rectangles: the table made for the first view is rejected
+    from yt_gb300.camera import Camera
+
+    moved = Camera(cam.position, cam.focus, (1.3, 1.3, 1.5), cam.resolution, lens_type=cam.lens_type)
+    assert np.array_equal(r.order(moved), order)
+    view2, _, _ = r.view_args(moved)
+    with pytest.raises(ValueError, match="another view"):
+        render(r.bricks, view2, order, _lib.VOLUME_RENDER,
+               torch.zeros((nx, ny, 4), dtype=torch.float64, device=cuda), tf=r.packed, tables=tables)

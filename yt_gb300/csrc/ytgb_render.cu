@@ -547,7 +547,10 @@ std::mutex g_noalloc_mutex;
 unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
 // The region's device address, looked up once per device with that device
-// current (the first call on a device does it).
+// current (the first call on a device does it).  cudaDeviceReset unloads
+// the module with the device's primary context; the address cached here is
+// then stale, so a process that resets a device does not call this entry
+// point on it again (stated in ytgb.h).
 int noalloc_scratch(unsigned char **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -573,6 +576,52 @@ int noalloc_scratch(unsigned char **out) {
     *out = g_noalloc_ptr[dev];
     return YTGB_OK;
 }
+
+
+// The host copy of a planned batch against the launch arguments: every
+// entry's arguments valid and of this sampler kind and table layout, the
+// shared memory enough for every entry's tables, and the tile numbering the
+// one ytgb_batch_plan writes for this tile shape.  The kernel stages each
+// entry's tables into smem_bytes of shared memory and maps work items to
+// tiles by this numbering, so a mismatch would write out of bounds or
+// mis-tile an image; with the table on the host it is checked for free.
+int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32_t ctf_fast, int32_t tile_shape,
+                       int32_t total_tiles, int32_t smem_bytes) {
+    const int TX = tile_shape == 1 ? 16 : (tile_shape == 2 ? 4 : 8);
+    const int TY = BLOCK / TX;
+    long long total = 0;
+    size_t smem = 0;
+    for (int32_t k = 0; k < n; k++) {
+        const ytgb_render_args &a = h[k].args;
+        if (int st = check_args(&a, false)) return st;
+        if (a.kind != kind || (kind == YTGB_VOLUME_RENDER && (a.tf.ctf_fast != 0) != (ctf_fast != 0))) {
+            ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
+                           " is not of the launch's sampler kind / table layout");
+            return YTGB_ERR_INVALID;
+        }
+        if (kind == YTGB_VOLUME_RENDER || kind == YTGB_LIGHT_SOURCE) {
+            size_t sm = 0;
+            if (int st = tf_check(a.tf, &sm, kind == YTGB_VOLUME_RENDER && ctf_fast != 0)) return st;
+            smem = sm > smem ? sm : smem;
+        }
+        const long long tx = (a.view.nx + TX - 1) / TX, ty = (a.view.ny + TY - 1) / TY;
+        if (h[k].tile_begin != total || h[k].tiles_y != ty || h[k].tiles != tx * ty) {
+            ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
+                           " is not planned for this tile shape (run ytgb_batch_plan with it)");
+            return YTGB_ERR_INVALID;
+        }
+        total += tx * ty;
+    }
+    if (total != total_tiles) {
+        ytgb_set_error("ytgb_batch_render_noalloc: total_tiles does not match the planned entries");
+        return YTGB_ERR_INVALID;
+    }
+    if ((size_t)smem_bytes < smem) {
+        ytgb_set_error("ytgb_batch_render_noalloc: smem_bytes is below what the entries' tables take");
+        return YTGB_ERR_INVALID;
+    }
+    return YTGB_OK;
+}
 }  // namespace
 
 extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind,
@@ -589,13 +638,16 @@ extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int3
         ytgb_set_error("ytgb_batch_render_noalloc: bad arguments");
         return YTGB_ERR_INVALID;
     }
+    if (int st = noalloc_check_plan(h_entries, n, kind, ctf_fast, tile_shape, total_tiles, smem_bytes)) return st;
     unsigned char *base = nullptr;
     if (int st = noalloc_scratch(&base)) return st;
     int32_t *queue = reinterpret_cast<int32_t *>(base);
     ytgb_batch_entry *entries = reinterpret_cast<ytgb_batch_entry *>(base + NOALLOC_QUEUE_BYTES);
     cudaStream_t s = (cudaStream_t)stream;
-    // the host table is consumed before the call returns (a copy from
-    // pageable memory is staged synchronously); the caller may reuse it
+    // A copy from pageable host memory is staged before cudaMemcpyAsync
+    // returns, so such a table may be reused at once; a page-locked table
+    // is read by the copy engine in stream order and must stay unchanged
+    // until the stream has passed this call (stated in ytgb.h).
     cudaError_t e = cudaMemcpyAsync(entries, h_entries, (size_t)n * sizeof(ytgb_batch_entry),
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof(int32_t), s);

@@ -17,6 +17,11 @@ over time.  The loop:
 * **drops** requests cancelled before their launch (``Request.cancelled``),
   releasing their budget; they are listed in ``server.cancelled``.
 
+With ``plain=True`` the same loop renders each request alone with the
+single-view kernel (``ytgb_render``), one launch per request on one stream,
+as yt renders one camera per ``Scene.render``: the comparator of the
+served form.
+
 Each request's image is exactly what rendering it alone gives (the same
 per-ray code, independent of the batch it lands in).
 """
@@ -30,6 +35,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .autotune import tile_shape_for
 from .batch import Batch, Job
 from .render import Renderer
 
@@ -62,19 +68,35 @@ class Request:
 
 @dataclass
 class _InFlight:
-    batch: Batch
     requests: list
     event: torch.cuda.Event
     stream: torch.cuda.Stream
     bytes: int
-    counters: torch.Tensor = field(default=None)
+    counters: torch.Tensor
+    error: torch.Tensor
+    keep: list = field(default_factory=list)   # device inputs the launch reads
+
+
+class _Plain:
+    """The counters and error word of one plain launch."""
+
+    def __init__(self, device):
+        self.counters = torch.zeros(4, dtype=torch.int64, device=device)
+        self.error = torch.zeros(1, dtype=torch.int32, device=device)
 
 
 class RenderServer:
     def __init__(self, volumes: dict, tfs: dict, device="cuda", hbm_budget=8 << 30, slots=4, max_batch=64,
-                 tile_shape=None, keep_images=False):
-        """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name -> transfer function."""
+                 tile_shape=None, keep_images=False, plain=False):
+        """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name ->
+        transfer function.  ``plain``: one single-view launch per request
+        on one stream (``slots`` and ``max_batch`` are then 1).
+        ``keep_images``: keep every finished request's image (True), none
+        (False), or those a predicate of the request selects."""
         self.device = torch.device(device)
+        self.plain = bool(plain)
+        if self.plain:
+            slots, max_batch = 1, 1
         self.renderers = {}
         self.volumes = {}
         from .transfer_functions import pack
@@ -105,6 +127,8 @@ class RenderServer:
         return r
 
     def _launch(self, reqs, stream, now):
+        if self.plain:
+            return self._launch_plain(reqs, stream, now)
         jobs = []
         for q in reqs:
             q.image = torch.empty((*q.camera.resolution, 4), dtype=torch.float64, device=self.device)
@@ -117,7 +141,29 @@ class RenderServer:
         ev.record(stream)
         for q in reqs:
             q.launched = now
-        return _InFlight(b, reqs, ev, stream, sum(q.image_bytes for q in reqs))
+        return _InFlight(reqs, ev, stream, sum(q.image_bytes for q in reqs), b.counters, b.error, [b])
+
+    def _launch_plain(self, reqs, stream, now):
+        from .volume import render as vrender
+
+        pl = _Plain(self.device)
+        keep = []
+        stream.wait_stream(torch.cuda.current_stream(self.device))
+        for q in reqs:
+            r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
+            with torch.cuda.stream(stream):
+                q.image = torch.zeros((*q.camera.resolution, 4), dtype=torch.float64, device=self.device)
+            view = q.camera.device_view()
+            ctf = bool(q.kind == _lib.VOLUME_RENDER and r.packed is not None and r.packed.header.ctf_fast)
+            ts = self.tile_shape if self.tile_shape is not None else tile_shape_for(q.kind, ctf, view.lens)
+            vrender(r.bricks, view, r.order(q.camera), q.kind, q.image,
+                    tf=r.packed if q.kind in (_lib.VOLUME_RENDER, _lib.LIGHT_SOURCE) else None,
+                    n_samples=q.n_samples, flags=int(ts) << _lib.FLAG_TILE_SHIFT, counters=pl.counters,
+                    error=pl.error, stream=stream, keep=keep)
+            q.launched = now
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        return _InFlight(reqs, ev, stream, sum(q.image_bytes for q in reqs), pl.counters, pl.error, keep)
 
     def run(self, requests, realtime=True, timeout=600.0):
         """Serve ``requests`` (sorted by arrival).  With ``realtime`` the
@@ -150,11 +196,12 @@ class RenderServer:
                     t = time.perf_counter() - t0
                     for q in f.requests:
                         q.done = t
-                        if not self.keep_images:
+                        keep = self.keep_images(q) if callable(self.keep_images) else self.keep_images
+                        if not keep:
                             q.image = None
                     self.in_use -= f.bytes
-                    self.samples += int(f.batch.counters[0].item())
-                    f.batch.check()
+                    self.samples += int(f.counters[0].item())
+                    _lib.check(_lib.lib().ytgb_check_error(f.error.data_ptr(), f.stream.cuda_stream), "serve")
                     free.append(f.stream)
                     inflight.remove(f)
                     done += f.requests

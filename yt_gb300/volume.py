@@ -434,15 +434,26 @@ def _table(rects: np.ndarray, order: np.ndarray) -> np.ndarray:
     return tab
 
 
+def _view_key(view: _lib.View) -> bytes:
+    """The view's geometry as bytes: every field the pixel rectangles depend
+    on (image size, lens, camera vectors, bounds, widths, camera data), not
+    the per-pixel ray pointers."""
+    return bytes(view)[: _lib.View.px_pos.offset]
+
+
 class RenderTables:
     """The table one render reads -- each order entry's pixel rectangle (4
-    int32), then the order -- on the device, with the host copy of the
-    order it was made for (the kernel indexes the bricks by the device
-    copy, so render() accepts it only for that same order)."""
+    int32), then the order -- on the device, with the host copies of the
+    order and of the view geometry it was made for.  The kernel indexes the
+    bricks by the device copy of the order and culls each brick to its
+    stored rectangle, so render() accepts the table only for that same order
+    and view: a camera that moved while the order stayed the same would
+    otherwise cull bricks from pixels they now cover."""
 
-    def __init__(self, table: torch.Tensor, order: np.ndarray):
+    def __init__(self, table: torch.Tensor, order: np.ndarray, view_key: bytes):
         self.table = table
         self.order = order.copy()
+        self.view_key = view_key
 
 
 def render_tables(bricks: BrickSet, view: _lib.View, order: np.ndarray, rects: np.ndarray | None = None
@@ -456,7 +467,7 @@ def render_tables(bricks: BrickSet, view: _lib.View, order: np.ndarray, rects: n
         rects = bricks.rects(view, order)
     if np.shape(rects) != (order.size, 4):
         raise ValueError("rects must hold 4 entries per order entry")
-    return RenderTables(torch.from_numpy(_table(rects, order)).to(bricks.device), order)
+    return RenderTables(torch.from_numpy(_table(rects, order)).to(bricks.device), order, _view_key(view))
 
 
 def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, image: torch.Tensor,
@@ -488,6 +499,8 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
         if (t is None or not np.array_equal(tables.order, order) or t.device.type != "cuda"
                 or (dev.index is not None and t.device.index != dev.index)):
             raise ValueError(f"tables must come from render_tables for this order, on {dev}")
+        if tables.view_key != _view_key(view):
+            raise ValueError("tables were made for another view: their pixel rectangles do not fit this camera")
         tab_d = t
     args = _lib.RenderArgs()
     args.kind = int(kind)
