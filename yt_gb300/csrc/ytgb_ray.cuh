@@ -168,6 +168,28 @@ YTGB_HD float diff_to_float(long long xb, long long yb) {
     return xb >= yb ? diff_to_float_ordered(xb, yb) : -diff_to_float_ordered(yb, xb);
 }
 
+// diff_to_float with its common case as selects: x, y normal, y >= 2^-74,
+// x < 2^73 and their exponents equal or adjacent (either order), the
+// difference of the significands scaled by the smaller exponent; anything
+// else takes diff_to_float.  The same value in every case.
+YTGB_HD float diff_to_float_sel(long long xb, long long yb) {
+    const bool ge = xb >= yb;
+    const long long hb = ge ? xb : yb, lb = ge ? yb : xb;
+    const int eh = (int)(hb >> 52), el = (int)(lb >> 52);
+    const int sh = eh - el;
+    if (!(el >= 949 && eh <= 1148 && sh <= 1)) return diff_to_float(xb, yb);
+    const unsigned long long mh = (unsigned long long)((hb & MANT52) | (1LL << 52));
+    const unsigned long long ml = (unsigned long long)((lb & MANT52) | (1LL << 52));
+    const unsigned long long F = (mh << sh) - ml;
+#ifdef __CUDA_ARCH__
+    const float f = __ull2float_rn(F);
+#else
+    const float f = (float)F;
+#endif
+    const float mag = fmul(f, ffrom((uint32_t)(el - 1075 + 127) << 23));
+    return ge ? mag : -mag;
+}
+
 // floor(ty) and ty - floor(ty) (as float) for a positive normal ty < 2^30.
 YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
     const int e = (int)(tb >> 52) - 1023;
@@ -881,6 +903,190 @@ YTGB_HD void advance_position(float P[3], const float vel[3], float dtf, int i, 
     else P[2] = wrap;
 }
 
+// Non-grey channel update of FIT_eval_transfer as selects (acc_emit without
+// its branch): d = 0 leaves the value unchanged.
+template <bool COMP>
+YTGB_HD void emit_sel(float &h, float &l, float d) {
+    float hh = h, ll = l;
+    if (COMP) {
+        const float u = fsub(fsub(1.0f, h), l);
+        acc_add(hh, ll, fmul(d, u));
+    } else {
+        hh = ffma(fsub(1.0f, d), h, d);
+    }
+    const bool small = d < 1.0f;
+    h = small ? hh : d;
+    l = small ? ll : 0.0f;
+}
+
+// Projection / interpolated-projection accumulation: x += inc.
+template <bool COMP>
+YTGB_HD void add_sel(float &h, float &l, float inc) {
+    if (COMP) acc_add(h, l, inc);
+    else h = fadd(h, inc);
+}
+
+// The cell loop of one walk for the common case: integer stepping (every
+// walk value positive and finite), one sample per cell, no mask, every
+// index of the entry cell inside the brick.  It visits the same cells with
+// the same enter/exit t and forms the same sample values and image updates
+// as sample_cell, operation for operation; what differs is the control
+// flow.  The choice of axis, the tmax update and the transfer function's
+// range test are selects, so one cell's body is a single straight run of
+// instructions in which the integer traversal and the float32 sampling can
+// be interleaved; only the rare cases (tmax leaving its binade, a step
+// count past the bound) branch.  Every entry index inside the brick stays
+// inside until the walk leaves it (an index changes only by a step on its
+// own axis, after which the exit test runs).
+template <int MODE, int CTF, bool COMP>
+YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, const ytgb_brick *bp,
+                        const CellCtx &c, const Walk &w, long long kmax, int step_limit, RayState &st) {
+    AxisStep A0, A1, A2;
+    A0.bits = dbits(w.tmax[0]);
+    A1.bits = dbits(w.tmax[1]);
+    A2.bits = dbits(w.tmax[2]);
+    {
+        // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
+        const double t0 = dmul(dmul((double)r.step[0], r.iv[0]), ldg(&bp->dds[0]));
+        const double t1 = dmul(dmul((double)r.step[1], r.iv[1]), ldg(&bp->dds[1]));
+        const double t2 = dmul(dmul((double)r.step[2], r.iv[2]), ldg(&bp->dds[2]));
+        step_prepare(A0, t0);
+        step_prepare(A1, t1);
+        step_prepare(A2, t2);
+    }
+    long long eb = dbits(w.enter_t);
+    float P0 = w.P[0], P1 = w.P[1], P2 = w.P[2];
+    int c0 = w.cur[0], c1 = w.cur[1], c2 = w.cur[2];
+    const float v0 = c.vel[0], v1 = c.vel[1], v2 = c.vel[2];
+    const float wr0 = r.step[0] > 0 ? 0.0f : 1.0f, wr1 = r.step[1] > 0 ? 0.0f : 1.0f,
+                wr2 = r.step[2] > 0 ? 0.0f : 1.0f;
+    const ytgb_tf &tf = a.tf;
+    const float nbm2 = (float)(tf.nbins[0] - 2);
+    const bool grey = tf.grey_opacity == 1;
+    unsigned nv = 0;
+    while (true) {
+        if (nv >= (unsigned)step_limit) {
+            set_error(a.error, YTGB_DEVERR_STEP_LIMIT);
+            break;
+        }
+        nv++;
+        // the axis of the smallest tmax, strict < ties (grid_traversal.pyx:122-131)
+        const bool lt01 = A0.bits < A1.bits, lt02 = A0.bits < A2.bits, lt12 = A1.bits < A2.bits;
+        const bool s0 = lt01 && lt02;
+        const bool s1 = !lt01 && lt12;
+        const bool s2 = !s0 && !s1;
+        const long long tmb = s0 ? A0.bits : (s1 ? A1.bits : A2.bits);
+        const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
+        const float dtf = diff_to_float_sel(xb, eb);
+        // the sample at the middle of the cell's segment (n_samples = 1)
+        const float f = fmul(dtf, 0.5f);
+        const float fx = cell_coord<true>(ffma(f, v0, P0));
+        const float fy = cell_coord<true>(ffma(f, v1, P1));
+        const float fz = cell_coord<true>(ffma(f, v2, P2));
+        const int off = c0 * c.sx + c1 * c.sy + c2;
+        if (MODE == MODE_VR && CTF) {
+            const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
+            const bool in = !(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val);
+            float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
+            q = fminf(fmaxf(q, 0.0f), nbm2);  // a NaN q gives bin 0 (the sample is then out of range)
+            const int bin = (int)q;
+            const float4 Y = s_tab[3 * bin + 0], D = s_tab[3 * bin + 1];
+            const float4 Z = s_tab[3 * bin + 2];
+            const float dd = fsub(fsub(val, Z.x), Z.y);
+            const float al = ffma(dd, D.w, Y.w);
+            const float er = fmul(ffma(dd, D.x, Y.x), al);
+            const float eg = fmul(ffma(dd, D.y, Y.y), al);
+            const float eb_ = fmul(ffma(dd, D.z, Y.z), al);
+            if (grey) {
+                float h[4] = {st.xh[0], st.xh[1], st.xh[2], st.xh[3]};
+                float l[4] = {st.xl[0], st.xl[1], st.xl[2], st.xl[3]};
+                const float da = fmul(dtf, al);
+                acc_grey(h[0], l[0], dtf, er, da, COMP);
+                acc_grey(h[1], l[1], dtf, eg, da, COMP);
+                acc_grey(h[2], l[2], dtf, eb_, da, COMP);
+                acc_grey(h[3], l[3], dtf, al, da, COMP);
+                YTGB_UNROLL
+                for (int ch = 0; ch < 4; ch++) {
+                    st.xh[ch] = in ? h[ch] : st.xh[ch];
+                    st.xl[ch] = in ? l[ch] : st.xl[ch];
+                }
+            } else {
+                emit_sel<COMP>(st.xh[0], st.xl[0], in ? fmul(dtf, er) : 0.0f);
+                emit_sel<COMP>(st.xh[1], st.xl[1], in ? fmul(dtf, eg) : 0.0f);
+                emit_sel<COMP>(st.xh[2], st.xl[2], in ? fmul(dtf, eb_) : 0.0f);
+            }
+        } else if (MODE == MODE_IPROJ) {
+            const int n3 = c.nf < 3 ? c.nf : 3;
+            YTGB_UNROLL
+            for (int ch = 0; ch < 3; ch++)
+                if (ch < n3)
+                    add_sel<COMP>(st.xh[ch], st.xl[ch],
+                                  fmul(trilinear(c.base + ch * c.fstride + off, c.sy, c.sx, fx, fy, fz), dtf));
+        } else if (MODE == MODE_PROJ || MODE == MODE_MIP) {
+            const int di = (c0 * c.dims[1] + c1) * c.dims[2] + c2;
+            const int nch = c.nf < 4 ? c.nf : 4;
+            YTGB_UNROLL
+            for (int ch = 0; ch < 4; ch++) {
+                if (ch < nch) {
+                    const float val = ldg(c.base + ch * c.fstride + di);
+                    if (MODE == MODE_PROJ) {
+                        add_sel<COMP>(st.xh[ch], st.xl[ch], fmul(val, dtf));
+                    } else {
+                        const bool up = val > st.xh[ch];
+                        st.xh[ch] = up ? val : st.xh[ch];
+                        st.xl[ch] = up ? 0.0f : st.xl[ch];
+                    }
+                }
+            }
+        }
+        // advance (grid_traversal.pyx:134-138): the position to the exit
+        // point, the stepped axis onto the next cell's entry face
+        P0 = s0 ? wr0 : ffma(dtf, v0, P0);
+        P1 = s1 ? wr1 : ffma(dtf, v1, P1);
+        P2 = s2 ? wr2 : ffma(dtf, v2, P2);
+        c0 += s0 ? r.step[0] : 0;
+        c1 += s1 ? r.step[1] : 0;
+        c2 += s2 ? r.step[2] : 0;
+        const long long inc = s0 ? A0.inc : (s1 ? A1.inc : A2.inc);
+        const int md = s0 ? A0.mode : (s1 ? A1.mode : A2.mode);
+        const int ex = s0 ? A0.ex : (s1 ? A1.ex : A2.ex);
+        long long nb = tmb + inc;
+        if (md == 2) nb += nb & 1;  // a tie: to the even neighbour
+        A0.bits = s0 ? nb : A0.bits;
+        A1.bits = s1 ? nb : A1.bits;
+        A2.bits = s2 ? nb : A2.bits;
+        if (md == 3 || (int)(nb >> 52) != ex) {
+            // tmax leaves its binade (or has no integer step): the float64 add
+            // (selects rather than r.iv[i]: a runtime index would put the ray in local memory)
+            const int i = s0 ? 0 : (s1 ? 1 : 2);
+            const int sti = s0 ? r.step[0] : (s1 ? r.step[1] : r.step[2]);
+            const double ivi = s0 ? r.iv[0] : (s1 ? r.iv[1] : r.iv[2]);
+            const double td = dmul(dmul((double)sti, ivi), ldg(&bp->dds[i]));
+            const long long sb = dbits(dadd(dfrom(tmb), td));
+            if (s0) {
+                A0.bits = sb;
+                step_prepare(A0, td);
+            } else if (s1) {
+                A1.bits = sb;
+                step_prepare(A1, td);
+            } else {
+                A2.bits = sb;
+                step_prepare(A2, td);
+            }
+        }
+        eb = tmb;
+        const int ci = s0 ? c0 : (s1 ? c1 : c2);
+        const int dci = s0 ? c.dims[0] : (s1 ? c.dims[1] : c.dims[2]);
+        if ((unsigned)ci >= (unsigned)dci || !(tmb < kmax)) break;  // ... or enter_t >= max_t
+    }
+    st.visits += nv;
+    if (nv) {
+        if (MODE == MODE_VR) st.touched |= a.tf.grey_opacity == 1 ? 0xfu : 0x7u;
+        else if (MODE == MODE_IPROJ) st.touched |= (1u << (c.nf < 3 ? c.nf : 3)) - 1u;
+        else st.touched |= (1u << (c.nf < 4 ? c.nf : 4)) - 1u;
+    }
+}
+
 // One brick of one ray: cast_through_kdtree's walk_volume call
 // (image_samplers.pyx:186) with the sampler callback inlined.
 // s_tab: the transfer-function table as staged in shared memory; bi: the
@@ -901,10 +1107,6 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     const long long kmax = dkey(st.max_t);
     Walk w;
     if (!walk_setup(bf, bp, a.bounds, r, ifd, max_t, kmax, w)) return;
-    // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
-    double tdelta[3];
-    YTGB_UNROLL
-    for (int i = 0; i < 3; i++) tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), ldg(&bp->dds[i]));
     st.walks++;
     CellCtx c;
     c.nf = ldg(&bp->n_fields);
@@ -922,7 +1124,19 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     int hitc = 0;
     const long long b0 = dbits(w.tmax[0]), b1 = dbits(w.tmax[1]), b2 = dbits(w.tmax[2]);
     const long long INF = 0x7ff0000000000000LL;
-    if (b0 > 0 && b1 > 0 && b2 > 0 && b0 < INF && b1 < INF && b2 < INF && kmax > 0) {
+    const bool int_path = b0 > 0 && b1 > 0 && b2 > 0 && b0 < INF && b1 < INF && b2 < INF && kmax > 0;
+    if (MODE != MODE_TRACE && MODE != MODE_LIGHT && (MODE != MODE_VR || CTF) && int_path && a.n_samples == 1 &&
+        (MODE != MODE_VR || c.moff < 0 || !a.masks) && (unsigned)w.cur[0] < (unsigned)c.dims[0] &&
+        (unsigned)w.cur[1] < (unsigned)c.dims[1] && (unsigned)w.cur[2] < (unsigned)c.dims[2]) {
+        if (st.comp) cells_fast<MODE, CTF, true>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        else cells_fast<MODE, CTF, false>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        return;
+    }
+    // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
+    double tdelta[3];
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), ldg(&bp->dds[i]));
+    if (int_path) {
         // ---- integer cell loop (positive walk values: key == bits) -----------
         AxisStep A0, A1, A2;
         A0.bits = b0;
