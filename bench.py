@@ -692,7 +692,7 @@ def run_projection(args):
     threads = os.cpu_count() or 1
     oracle_imgs = {}
     t_or = 0.0
-    for v, comp, entry, out in views:
+    for v, comp, entry, out in ([] if args.no_cpu_baseline else views):
         key = id(v)
         if key not in oracle_imgs:
             p = v.camera.sampler_params()

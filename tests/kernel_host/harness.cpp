@@ -114,8 +114,7 @@ extern "C" long long emu_check_step(long long n, int steps, unsigned long long s
 }
 
 // mismatches of diff_to_float against (float)(x - y) computed in long double
-// (exact for these inputs), of diff_to_float_sel against diff_to_float, and
-// of split_floor against floor / fraction
+// (exact for these inputs), and of split_floor against floor / fraction
 extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
     std::mt19937_64 g(seed);
     long long bad = 0;
@@ -125,9 +124,6 @@ extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
         float got = diff_to_float(dbits(x), dbits(y));
         float want = (float)((long double)x - (long double)y);
         if (got != want) bad++;
-        // the select form of the fast cell loop: the same value, sign of zero included
-        float sel = diff_to_float_sel(dbits(x), dbits(y));
-        if (std::memcmp(&sel, &got, sizeof(float)) != 0) bad++;
         double t = std::ldexp((double)(g() >> 11), -(int)(g() % 60));  // 0 <= t < 2^53 .. small
         if (t > 0 && t < 1073741824.0) {
             int fl; float fr;

@@ -168,28 +168,6 @@ YTGB_HD float diff_to_float(long long xb, long long yb) {
     return xb >= yb ? diff_to_float_ordered(xb, yb) : -diff_to_float_ordered(yb, xb);
 }
 
-// diff_to_float with its common case as selects: x, y normal, y >= 2^-74,
-// x < 2^73 and their exponents equal or adjacent (either order), the
-// difference of the significands scaled by the smaller exponent; anything
-// else takes diff_to_float.  The same value in every case.
-YTGB_HD float diff_to_float_sel(long long xb, long long yb) {
-    const bool ge = xb >= yb;
-    const long long hb = ge ? xb : yb, lb = ge ? yb : xb;
-    const int eh = (int)(hb >> 52), el = (int)(lb >> 52);
-    const int sh = eh - el;
-    if (!(el >= 949 && eh <= 1148 && sh <= 1)) return diff_to_float(xb, yb);
-    const unsigned long long mh = (unsigned long long)((hb & MANT52) | (1LL << 52));
-    const unsigned long long ml = (unsigned long long)((lb & MANT52) | (1LL << 52));
-    const unsigned long long F = (mh << sh) - ml;
-#ifdef __CUDA_ARCH__
-    const float f = __ull2float_rn(F);
-#else
-    const float f = (float)F;
-#endif
-    const float mag = fmul(f, ffrom((uint32_t)(el - 1075 + 127) << 23));
-    return ge ? mag : -mag;
-}
-
 // floor(ty) and ty - floor(ty) (as float) for a positive normal ty < 2^30.
 YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
     const int e = (int)(tb >> 52) - 1023;
@@ -932,10 +910,10 @@ YTGB_HD void add_sel(float &h, float &l, float inc) {
 // the same enter/exit t and forms the same sample values and image updates
 // as sample_cell, operation for operation; what differs is the control
 // flow.  The choice of axis, the tmax update and the transfer function's
-// range test are selects, so one cell's body is a single straight run of
+// range test are selects, so one cell's body is a nearly straight run of
 // instructions in which the integer traversal and the float32 sampling can
-// be interleaved; only the rare cases (tmax leaving its binade, a step
-// count past the bound) branch.  Every entry index inside the brick stays
+// be interleaved; only the exponent cases of the dt conversion and the rare
+// cases (tmax leaving its binade, a step count past the bound) branch.  Every entry index inside the brick stays
 // inside until the walk leaves it (an index changes only by a step on its
 // own axis, after which the exit test runs).
 template <int MODE, int CTF, bool COMP>
@@ -977,7 +955,7 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
         const bool s2 = !s0 && !s1;
         const long long tmb = s0 ? A0.bits : (s1 ? A1.bits : A2.bits);
         const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
-        const float dtf = diff_to_float_sel(xb, eb);
+        const float dtf = diff_to_float(xb, eb);
         // the sample at the middle of the cell's segment (n_samples = 1)
         const float f = fmul(dtf, 0.5f);
         const float fx = cell_coord<true>(ffma(f, v0, P0));
