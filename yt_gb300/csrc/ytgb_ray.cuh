@@ -598,6 +598,27 @@ YTGB_HD void light_gradient(const float *__restrict__ p, const float *__restrict
     }
 }
 
+// One bin of the packed ColorTransferFunction tables: the four tables' y and
+// dy, and the bin's d0 as a float pair.  TG false: the block's shared-memory
+// copy, repacked as three float4 per bin (y[4], dy[4], d0); TG true: the
+// tables where ytgb_tf_pack left them in global memory, one float4
+// {y, dy, d0_hi, d0_lo} per table and bin (four cached loads).
+template <bool TG>
+YTGB_HD void ctf_bin(const float4 *__restrict__ tab, int nbins, int bin, float4 &Y, float4 &D, float2 &Z) {
+    if (TG) {
+        const float4 t0 = ldg(tab + bin), t1 = ldg(tab + nbins + bin);
+        const float4 t2 = ldg(tab + 2 * nbins + bin), t3 = ldg(tab + 3 * nbins + bin);
+        Y = make_float4(t0.x, t1.x, t2.x, t3.x);
+        D = make_float4(t0.y, t1.y, t2.y, t3.y);
+        Z = make_float2(t3.z, t3.w);
+    } else {
+        Y = tab[3 * bin + 0];
+        D = tab[3 * bin + 1];
+        const float4 z = tab[3 * bin + 2];
+        Z = make_float2(z.x, z.y);
+    }
+}
+
 // FIT_get_value + FIT_eval_transfer's table combination
 // (field_interpolation_tables.pxd:66-101).  The bounds test uses the float
 // nearest outside each bound, so for a float v it decides exactly as the
@@ -702,7 +723,7 @@ YTGB_HD float cell_coord(float x) {
     return CLAMP ? fminf(fmaxf(x, 0.0f), 1.0f) : x;
 }
 
-template <int MODE, int CTF, bool CLAMP = true>
+template <int MODE, int CTF, bool CLAMP = true, bool TG = false>
 YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi, const CellCtx &c, const int cur[3],
                          const float P[3], float dtf, long long enter_bits, long long exit_bits, RayState &st) {
     st.visits++;
@@ -801,8 +822,9 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
                 float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
                 q = fminf(fmaxf(q, 0.0f), (float)(tf.nbins[0] - 2));
                 const int bin = (int)q;
-                const float4 Y = s_tab[3 * bin + 0], D = s_tab[3 * bin + 1];
-                const float4 Z = s_tab[3 * bin + 2];
+                float4 Y, D;
+                float2 Z;
+                ctf_bin<TG>(s_tab, tf.nbins_max, bin, Y, D, Z);
                 const float dd = fsub(fsub(val, Z.x), Z.y);
                 const float al = ffma(dd, D.w, Y.w);
                 const float er = fmul(ffma(dd, D.x, Y.x), al);
@@ -916,7 +938,7 @@ YTGB_HD void add_sel(float &h, float &l, float inc) {
 // cases (tmax leaving its binade, a step count past the bound) branch.  Every entry index inside the brick stays
 // inside until the walk leaves it (an index changes only by a step on its
 // own axis, after which the exit test runs).
-template <int MODE, int CTF, bool COMP>
+template <int MODE, int CTF, bool COMP, bool TG>
 YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, const ytgb_brick *bp,
                         const CellCtx &c, const Walk &w, long long kmax, int step_limit, RayState &st) {
     AxisStep A0, A1, A2;
@@ -968,8 +990,9 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
             float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
             q = fminf(fmaxf(q, 0.0f), nbm2);  // a NaN q gives bin 0 (the sample is then out of range)
             const int bin = (int)q;
-            const float4 Y = s_tab[3 * bin + 0], D = s_tab[3 * bin + 1];
-            const float4 Z = s_tab[3 * bin + 2];
+            float4 Y, D;
+            float2 Z;
+            ctf_bin<TG>(s_tab, tf.nbins_max, bin, Y, D, Z);
             const float dd = fsub(fsub(val, Z.x), Z.y);
             const float al = ffma(dd, D.w, Y.w);
             const float er = fmul(ffma(dd, D.x, Y.x), al);
@@ -1067,9 +1090,10 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
 
 // One brick of one ray: cast_through_kdtree's walk_volume call
 // (image_samplers.pyx:186) with the sampler callback inlined.
-// s_tab: the transfer-function table as staged in shared memory; bi: the
-// brick index.
-template <int MODE, int CTF>
+// s_tab: the transfer-function tables -- as staged in shared memory (TG
+// false) or as packed in global memory (TG true, see ctf_bin); bi: the brick
+// index.
+template <int MODE, int CTF, bool TG = false>
 YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, int bi, RayState &st) {
     const ytgb_brick *bp = a.bricks + bi;
     BrickF bf;
@@ -1106,8 +1130,8 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     if (MODE != MODE_TRACE && MODE != MODE_LIGHT && (MODE != MODE_VR || CTF) && int_path && a.n_samples == 1 &&
         (MODE != MODE_VR || c.moff < 0 || !a.masks) && (unsigned)w.cur[0] < (unsigned)c.dims[0] &&
         (unsigned)w.cur[1] < (unsigned)c.dims[1] && (unsigned)w.cur[2] < (unsigned)c.dims[2]) {
-        if (st.comp) cells_fast<MODE, CTF, true>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
-        else cells_fast<MODE, CTF, false>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        if (st.comp) cells_fast<MODE, CTF, true, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        else cells_fast<MODE, CTF, false, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
         return;
     }
     // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
@@ -1135,7 +1159,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
             const long long tmb = i == 0 ? A0.bits : (i == 1 ? A1.bits : A2.bits);
             const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
             const float dtf = MODE == MODE_TRACE ? 0.0f : diff_to_float(xb, eb);
-            sample_cell<MODE, CTF>(a, s_tab, bi, c, w.cur, w.P, dtf, eb, xb, st);
+            sample_cell<MODE, CTF, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, eb, xb, st);
             // advance (grid_traversal.pyx:134-138)
             const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
             advance_position(w.P, c.vel, dtf, i, si);
@@ -1176,7 +1200,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
         const long long Ki = i == 0 ? K0 : (i == 1 ? K1 : K2);
         const double exit_t = Ki < kmax ? tm : max_t;
         const float dtf = MODE == MODE_TRACE ? 0.0f : (float)dsub(exit_t, enter_t);
-        sample_cell<MODE, CTF>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
+        sample_cell<MODE, CTF, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
         const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
         advance_position(w.P, c.vel, dtf, i, si);
         const double td = i == 0 ? tdelta[0] : (i == 1 ? tdelta[1] : tdelta[2]);

@@ -69,63 +69,64 @@ constexpr int NWARP = BLOCK / 32;
 // 2.67 ms -> 2.10 ms on the 1024^2 AMR frame, identical images.
 constexpr int MIN_BLOCKS = 5;
 
+// Selected bricks a warp holds before walking them (flushed in order when
+// nearly full).
+constexpr int SEL_CAP = 128;
+
 struct TileSmem {
-    unsigned long long cnt[4];
-    int sel[BLOCK];
-    int wsum[NWARP];
-    const float *tab_src;  // tables currently staged in s_tab
-    int tab_ctf;
-    int item;
+    Ray ray[BLOCK];                // each thread's ray, read per brick walk instead of held in registers
+    int sel[NWARP][SEL_CAP];       // each warp's selected order entries
 };
 
-// One tile of one view: cast_through_kdtree (image_samplers.pyx:146-197) for
-// every brick of the view, restricted to this tile's pixels.  The ordered
-// brick list is binned against the tile by the bricks' pixel rectangles
-// (ballot + prefix in shared memory, BLOCK bricks per pass, order kept); each
-// ray then walks the selected bricks whose rectangle holds its pixel.
-template <int MODE, int CTF, int TS>
-__device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, int by, float4 *s_tab, TileSmem &sm,
-                                            unsigned long long *hashes, long long *counts) {
-    constexpr int TX = TileShape<TS>::X, TY = TileShape<TS>::Y;
-    const ytgb_view &v = a.view;
-    const int tid = threadIdx.x;
-    if (tid < 4) sm.cnt[tid] = 0;
-    if (MODE == MODE_VR || MODE == MODE_LIGHT) {
-        // stage the transfer function unless this block already holds it
-        const float *src = a.tf_tables;
-        const bool reload = sm.tab_src != src || sm.tab_ctf != CTF;
-        if (reload) {
-            const float4 *g = reinterpret_cast<const float4 *>(src);
-            const int nb = a.tf.nbins_max;
-            if (CTF) {
-                for (int b = tid; b < nb; b += BLOCK) {
-                    float4 t0 = __ldg(g + 0 * nb + b), t1 = __ldg(g + 1 * nb + b);
-                    float4 t2 = __ldg(g + 2 * nb + b), t3 = __ldg(g + 3 * nb + b);
-                    s_tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
-                    s_tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
-                    s_tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
-                }
-            } else {
-                const int n = a.tf.n_fits * nb;
-                for (int k = tid; k < n; k += BLOCK) s_tab[k] = __ldg(g + k);
-            }
+// Stage the transfer function of a volume-rendering view in shared memory:
+// the ColorTransferFunction layout repacked as y[4], dy[4], d0 per bin (one
+// bin lookup serves all four tables), other table sets as they are.
+template <int CTF>
+__device__ __forceinline__ void stage_tf(const ytgb_render_args &a, float4 *s_tab) {
+    const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
+    const int nb = a.tf.nbins_max;
+    if (CTF) {
+        for (int b = threadIdx.x; b < nb; b += BLOCK) {
+            float4 t0 = __ldg(g + 0 * nb + b), t1 = __ldg(g + 1 * nb + b);
+            float4 t2 = __ldg(g + 2 * nb + b), t3 = __ldg(g + 3 * nb + b);
+            s_tab[3 * b + 0] = make_float4(t0.x, t1.x, t2.x, t3.x);
+            s_tab[3 * b + 1] = make_float4(t0.y, t1.y, t2.y, t3.y);
+            s_tab[3 * b + 2] = make_float4(t3.z, t3.w, 0.f, 0.f);
         }
-        __syncthreads();
-        if (tid == 0) {
-            sm.tab_src = src;
-            sm.tab_ctf = CTF;
-        }
+    } else {
+        const int n = a.tf.n_fits * nb;
+        for (int k = threadIdx.x; k < n; k += BLOCK) s_tab[k] = __ldg(g + k);
     }
-    __syncthreads();
+}
 
-    const int vj = by * TY + (tid % TY);
-    const int vi = bx * TX + (tid / TY);
+// One warp's 32 pixels of one tile of one view: cast_through_kdtree
+// (image_samplers.pyx:146-197) for every brick of the view, restricted to
+// these pixels.  The warp bins the ordered brick list against its pixels'
+// rectangle 32 bricks at a time (one per lane: ballot and prefix count into
+// the warp's list, order kept) and walks the list whenever it is nearly full
+// and at the end; each ray walks the listed bricks whose pixel rectangle
+// holds its pixel.  Nothing waits on other warps, so a warp whose rays end
+// early takes its next work at once.
+//   bx, by: the block tile (TX x TY pixels); w: which 32 of its 128 pixels;
+//   tab: the transfer-function tables (shared: TG false; global: TG true);
+//   slot: this thread's ray slot in sm.ray, wl: its warp's list in sm.sel.
+template <int MODE, int CTF, int TS, bool TG>
+__device__ __forceinline__ void warp_tile(const ytgb_render_args &a, int bx, int by, int w, const float4 *tab,
+                                          TileSmem &sm, int slot, int wl, unsigned long long *hashes,
+                                          long long *counts) {
+    constexpr int TX = TileShape<TS>::X, TY = TileShape<TS>::Y;
+    constexpr int WROWS = 32 / TY;  // image rows of a warp's pixels
+    const ytgb_view &v = a.view;
+    const int lane = threadIdx.x & 31;
+    const int t = w * 32 + lane;  // the pixel within the block tile
+    const int vj = by * TY + (t % TY);
+    const int vi = bx * TX + (t / TY);
     const bool active = vi < v.nx && vj < v.ny;
-    const int tx0 = bx * TX, tx1 = tx0 + TX;
-    const int ty0 = by * TY, ty1 = ty0 + TY;
+    const int r0 = bx * TX + w * WROWS, r1 = r0 + WROWS;  // the warp's pixel rectangle
+    const int c0 = by * TY, c1 = c0 + TY;
     const size_t p = active ? (size_t)vi * v.ny + vj : 0;
 
-    Ray r;
+    Ray &r = sm.ray[slot];
     if (active) make_ray(v, vi, vj, r);
     double *img = a.image + p * 4;
     RayState st;
@@ -137,32 +138,29 @@ __device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, i
     }
     const int4 *rects = reinterpret_cast<const int4 *>(a.rects);
     const int n_order = a.n_order;
-    for (int base = 0; base < n_order; base += BLOCK) {
-        const int k = base + tid;
+    int *sel = sm.sel[wl];
+    int nsel = 0;  // the same in every lane
+    for (int base = 0; base < n_order; base += 32) {
+        const int k = base + lane;
         bool hit = false;
         if (k < n_order) {
             const int4 rc = __ldg(rects + k);
-            hit = rc.x < tx1 && rc.y > tx0 && rc.z < ty1 && rc.w > ty0;
+            hit = rc.x < r1 && rc.y > r0 && rc.z < c1 && rc.w > c0;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        const int lane = tid & 31, wid = tid >> 5;
-        if (lane == 0) sm.wsum[wid] = __popc(bal);
-        __syncthreads();
-        int off = 0, nsel = 0;
-#pragma unroll
-        for (int q = 0; q < NWARP; q++) {
-            off += q < wid ? sm.wsum[q] : 0;
-            nsel += sm.wsum[q];
+        if (hit) sel[nsel + __popc(bal & ((1u << lane) - 1u))] = k;
+        nsel += __popc(bal);
+        if (nsel > SEL_CAP - 32 || base + 32 >= n_order) {
+            __syncwarp();
+            for (int j = 0; active && j < nsel; j++) {
+                const int kk = sel[j];
+                const int4 rc = __ldg(rects + kk);
+                if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
+                walk_brick<MODE, CTF, TG>(a, tab, r, __ldg(a.order + kk), st);
+            }
+            __syncwarp();  // the list is rewritten by the next passes
+            nsel = 0;
         }
-        if (hit) sm.sel[off + __popc(bal & ((1u << lane) - 1u))] = k;
-        __syncthreads();
-        for (int j = 0; active && j < nsel; j++) {
-            const int kk = sm.sel[j];
-            const int4 rc = __ldg(rects + kk);
-            if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
-            walk_brick<MODE, CTF>(a, s_tab, r, __ldg(a.order + kk), st);
-        }
-        __syncthreads();  // sel / wsum are rewritten by the next pass
     }
 
     if (active) {
@@ -176,73 +174,66 @@ __device__ __forceinline__ void render_tile(const ytgb_render_args &a, int bx, i
         }
     }
     if (a.counters) {
-        if (st.visits) atomicAdd(&sm.cnt[0], (unsigned long long)st.visits);
-        if (st.walks) atomicAdd(&sm.cnt[1], (unsigned long long)st.walks);
-        if (st.guarded) atomicAdd(&sm.cnt[3], (unsigned long long)st.guarded);
-        if (active) atomicAdd(&sm.cnt[2], 1ull);
-        __syncthreads();
-        if (tid < 4 && sm.cnt[tid]) atomicAdd(a.counters + tid, sm.cnt[tid]);
+        // per warp: one sum per counter, one atomic per counter
+        const unsigned sv = __reduce_add_sync(0xffffffffu, st.visits);
+        const unsigned sw = __reduce_add_sync(0xffffffffu, st.walks);
+        const unsigned sg = __reduce_add_sync(0xffffffffu, st.guarded);
+        const unsigned sr = __popc(__ballot_sync(0xffffffffu, active));
+        if (lane == 0) {
+            if (sv) atomicAdd(a.counters + 0, (unsigned long long)sv);
+            if (sw) atomicAdd(a.counters + 1, (unsigned long long)sw);
+            if (sr) atomicAdd(a.counters + 2, (unsigned long long)sr);
+            if (sg) atomicAdd(a.counters + 3, (unsigned long long)sg);
+        }
     }
-    __syncthreads();
 }
 
-// One view, one tile per block.
+// One view, one tile per block (four warps of 32 pixels).
 template <int MODE, int CTF, int TS>
 __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
                                                        long long *counts) {
     extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;
-    if (threadIdx.x == 0) {
-        sm.tab_src = nullptr;
-        sm.tab_ctf = -1;
+    if (MODE == MODE_VR || MODE == MODE_LIGHT) {
+        stage_tf<CTF>(a, s_tab);
+        __syncthreads();
     }
-    __syncthreads();
-    render_tile<MODE, CTF, TS>(a, blockIdx.y, blockIdx.x, s_tab, sm, hashes, counts);
+    const int w = threadIdx.x >> 5;
+    warp_tile<MODE, CTF, TS, false>(a, blockIdx.y, blockIdx.x, w, s_tab, sm, threadIdx.x, w, hashes, counts);
 }
 
-// The batch kernel renders each work item through this out-of-line copy of
-// render_tile.  With render_tile inlined into the persistent loop, sm_103a
-// builds of the interpolated-projection sampler produced images that differed
-// from render_kernel's under some optimisation settings (-O3, ptxas -O1, the
-// launch arguments staged in shared memory) and not under others; the cause
-// was not identified.  Called out of line, every sampler, tile shape and
-// block count tested matches render_kernel bit for bit.  One call per tile
-// costs nothing measurable.
-template <int MODE, int CTF, int TS>
-__device__ __noinline__ void render_tile_outlined(const ytgb_render_args &a, int bx, int by, float4 *s_tab,
-                                                  TileSmem &sm) {
-    render_tile<MODE, CTF, TS>(a, bx, by, s_tab, sm, nullptr, nullptr);
-}
-
-// Many views in one persistent launch: blocks pull (view, tile) work items
-// from a device counter until the batch is drained, so small and large views
-// share the GPU without a launch per view.  Entries are sorted by
-// tile_begin; an item's view is found by binary search.
+// Many views in one persistent launch: every warp pulls work items -- one
+// warp's 32 pixels of a (view, tile) -- from a device counter until the
+// batch is drained, so small and large views share the GPU without a launch
+// per view and no warp waits for another.  An item's view is found by binary
+// search over the entries' first tiles.  Views may use different transfer
+// functions, so the tables are read from global memory (cached), not staged.
+// Every loop iteration takes a new item: a warp runs at most as many
+// iterations as there are items (no spin, no barrier).
 template <int MODE, int CTF, int TS>
 __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
                                                       int total_tiles, int *queue) {
-    extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;
-    if (threadIdx.x == 0) {
-        sm.tab_src = nullptr;
-        sm.tab_ctf = -1;
-    }
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const long long total_items = (long long)total_tiles * NWARP;
     while (true) {
-        if (threadIdx.x == 0) sm.item = atomicAdd(queue, 1);
-        __syncthreads();
-        const int item = sm.item;
-        __syncthreads();
-        if (item >= total_tiles) break;
+        int item = 0;
+        if (lane == 0) item = atomicAdd(queue, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item < 0 || item >= total_items) break;
+        const int tile = item / NWARP;
         int lo = 0, hi = n_entries - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(&entries[mid].tile_begin) <= item) lo = mid;
+            if (__ldg(&entries[mid].tile_begin) <= tile) lo = mid;
             else hi = mid - 1;
         }
         const ytgb_batch_entry &e = entries[lo];
-        const int t = item - __ldg(&e.tile_begin);
+        const int t = tile - __ldg(&e.tile_begin);
         const int ty = __ldg(&e.tiles_y);
-        render_tile_outlined<MODE, CTF, TS>(e.args, t / ty, t % ty, s_tab, sm);
+        warp_tile<MODE, CTF, TS, true>(e.args, t / ty, t % ty, item % NWARP,
+                                       reinterpret_cast<const float4 *>(e.args.tf_tables), sm, threadIdx.x, wl,
+                                       nullptr, nullptr);
     }
 }
 
@@ -381,18 +372,19 @@ int launch_ts(int ts, const ytgb_render_args *a, size_t smem, cudaStream_t s, un
 int tile_shape_of(uint32_t flags) { return (int)((flags >> YTGB_FLAG_TILE_SHIFT) & 0xfu); }
 
 template <int MODE, int CTF, int TS>
-int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem, cudaStream_t s) {
-    if (int st = set_smem(batch_kernel<MODE, CTF, TS>, smem)) return st;
+int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t, cudaStream_t s) {
+    // the batch reads its transfer functions from global memory: no dynamic
+    // shared memory (the planned smem_bytes is what render_kernel stages)
     if (blocks <= 0) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, CTF, TS>, BLOCK, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, CTF, TS>, BLOCK, 0);
         blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
     if (blocks > total) blocks = total;
     if (blocks < 1) blocks = 1;
-    batch_kernel<MODE, CTF, TS><<<blocks, BLOCK, smem, s>>>(d, n, total, queue);
+    batch_kernel<MODE, CTF, TS><<<blocks, BLOCK, 0, s>>>(d, n, total, queue);
     return launch_status("batch launch");
 }
 
@@ -474,7 +466,7 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
         entries[k].tiles_y = ty;
         entries[k].tiles = tx * ty;
         total += (long long)tx * ty;
-        if (total > 0x7fffffff) {
+        if (total * NWARP > 0x7fff0000LL) {  // warp work items count in an int32
             ytgb_set_error("ytgb_batch_plan: too many tiles");
             return YTGB_ERR_INVALID;
         }
