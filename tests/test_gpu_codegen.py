@@ -1,0 +1,106 @@
+"""The same images whatever the kernels' register budget.
+
+Every float operation of the samplers is an explicit round-to-nearest
+intrinsic (and the float64 walk is never contracted), so how the compiler
+allocates registers, schedules or spills must not change a single bit.  This
+test compiles a second copy of the sampler kernels for 4 resident blocks per
+SM (128 registers a thread) instead of the library's 5 (96), loads it beside
+the library, and renders every sampler path through both: the persistent
+batch kernel and the single-view kernel of either build give bit-identical
+images, and one view matches the float64 oracle.
+"""
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpu as ocpu
+from test_gpu_batch import cams, mv_tf, same_bits
+from yt_gb300 import _lib, testing, workloads
+from yt_gb300.amr_kdtree import AMRKDTree
+from yt_gb300.batch import Batch, Job
+from yt_gb300.render import Renderer, relative_error
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+CSRC = ROOT / "yt_gb300" / "csrc"
+
+
+@pytest.fixture(scope="module")
+def variant(cuda, tmp_path_factory):
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    d = tmp_path_factory.mktemp("ytgb_regs128")
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              f"-I{ROOT / 'include'}", f"-I{CSRC}"]
+    arch = ["-gencode", "arch=compute_103a,code=sm_103a"]
+    subprocess.run([nvcc, *arch, "--fmad=false", "-DYTGB_MIN_BLOCKS=4", *common, "-c", str(CSRC / "ytgb_render.cu"),
+                    "-o", str(d / "r.o")], check=True)
+    subprocess.run([nvcc, *common, "-c", str(CSRC / "ytgb_host.cpp"), "-o", str(d / "h.o")], check=True)
+    so = d / "libytgb_regs128.so"
+    subprocess.run([nvcc, *arch, "-shared", "-o", str(so), str(d / "r.o"), str(d / "h.o"), "-lcudart", "-Xcompiler",
+                    "-pthread"], check=True)
+    V = C.CDLL(str(so))
+    for name, (res, args) in _lib.SIGNATURES.items():
+        fn = getattr(V, name, None)
+        if fn is not None:
+            fn.restype, fn.argtypes = res, args
+    return V
+
+
+def test_other_register_budget_same_images(cuda, variant):
+    grids = testing.amr_blob_grids(root=32, levels=2, patch=8, seed=0)
+    kd = AMRKDTree(grids, log_field=False)
+    bricks = kd.bricks()
+    two = [([d[0], np.sqrt(np.abs(d[0]))], m, le, re, dims) for d, m, le, re, dims in bricks]
+    lo = float(min(np.min(d[0]) for d, *_ in bricks))
+    hi = float(max(np.max(d[0]) for d, *_ in bricks))
+    r_mv = Renderer(two, mv_tf(lo, hi), device=cuda, kdtree=kd)
+    r_lin = Renderer(bricks, None, device=cuda, kdtree=kd)
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
+    r_ctf = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
+    cases = [(r_ctf, _lib.VOLUME_RENDER, 1), (r_mv, _lib.VOLUME_RENDER, 2), (r_lin, _lib.PROJECTION, 1),
+             (r_lin, _lib.INTERPOLATED_PROJECTION, 3), (r_lin, _lib.MIP, 1), (r_ctf, _lib.LIGHT_SOURCE, 2)]
+    light = ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0))
+    jobs = [Job(r, cam, kind, n_samples=ns, light=light if kind == _lib.LIGHT_SOURCE else None)
+            for (r, kind, ns) in cases for cam in cams(4, seed=3)]
+    b = Batch(jobs, device=cuda)
+    b.launch()
+    torch.cuda.synchronize()
+    b.check()
+    ref = [im.clone() for im in b.images]
+    # the same planned batch through the other build
+    for im in b.images:
+        im.zero_()
+    stream = torch.cuda.current_stream(cuda)
+    for q, g in enumerate(b.groups):
+        st = variant.ytgb_batch_render(g.dev.data_ptr(), g.n, g.kind, g.ctf, b.tile_shape, g.total_tiles, g.smem,
+                                       b.queue.data_ptr() + 4 * q, 0, C.c_void_p(stream.cuda_stream))
+        assert st == _lib.OK, variant.ytgb_last_error()
+    torch.cuda.synchronize()
+    b.check()
+    for j, want in zip(jobs, ref):
+        assert same_bits(j.image, want), (j.kind, j.n_samples)
+    # single views through the other build's render_kernel
+    saved = _lib._lib
+    try:
+        _lib._lib = variant
+        other = [j.renderer.render(j.camera, kind=j.kind, n_samples=j.n_samples, light=j.light) for j in jobs]
+        torch.cuda.synchronize()
+    finally:
+        _lib._lib = saved
+    for j, img in zip(jobs, other):
+        assert same_bits(img, j.image), (j.kind, j.n_samples)
+    # and one of them against the float64 oracle
+    j = jobs[0]
+    p = j.camera.sampler_params()
+    s = ocpu.OracleSampler("volume_render", p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], p["image"],
+                           p["x_vec"], p["y_vec"], p["width"], lens_type=p["lens_type"],
+                           camera_data=p["camera_data"], tf=w.tf)
+    s.render(ocpu.OracleBricks(w.bricks), r_ctf.order(j.camera))
+    assert relative_error(j.image.cpu().numpy(), p["image"], channels=(0, 1, 2))[0] <= 1e-5

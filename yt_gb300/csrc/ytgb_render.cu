@@ -3,9 +3,10 @@
 // One CUDA thread owns one pixel ray for the whole launch and walks every
 // brick of the view in the kd viewpoint order, so the per-brick Python loop,
 // OpenMP region and image read/write of yt's cast_through_kdtree
-// (image_samplers.pyx:146-197) disappear.  Each block bins the ordered brick
-// list against its 8x16 pixel tile (the bricks' pixel rectangles) in shared
-// memory, so a ray only looks at bricks whose rectangle can contain it.
+// (image_samplers.pyx:146-197) disappear.  Each warp bins the ordered brick
+// list against its 32 pixels (the bricks' pixel rectangles) into a list in
+// shared memory, so a ray only looks at bricks whose rectangle can contain
+// it, and no warp waits for another.
 //
 // Precision split.  The cell walk of walk_volume (grid_traversal.pyx:26-140)
 // is reproduced bit for bit: every float64 value the walk compares or hands
@@ -64,10 +65,15 @@ constexpr int BLOCK = 128;
 constexpr int NWARP = BLOCK / 32;
 // Resident blocks per SM the kernels are compiled for (at most 96 registers
 // a thread).  The per-ray walk is latency-bound (dependent integer and
-// float64 steps); 20 warps per SM hide more of that latency than the 12 the
-// unconstrained build (154 registers) allows, despite some spilling:
-// 2.67 ms -> 2.10 ms on the 1024^2 AMR frame, identical images.
-constexpr int MIN_BLOCKS = 5;
+// float64 steps), so warps per SM count for more than registers: with the
+// rays held in shared memory the 96-register build does not spill, and on
+// the 1024^2 AMR frame it runs 1.30 ms against 1.28 ms at 6 blocks (80
+// registers, spilling) and 1.42 ms at 7; the 64-view batch prefers 5 (37.0
+// against 40.0 and 39.0 ms).  Images are identical at every setting.
+#ifndef YTGB_MIN_BLOCKS
+#define YTGB_MIN_BLOCKS 5
+#endif
+constexpr int MIN_BLOCKS = YTGB_MIN_BLOCKS;
 
 // Selected bricks a warp holds before walking them (flushed in order when
 // nearly full).
