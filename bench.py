@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="default line without the batched record")
     ap.add_argument("--no-served", action="store_true", help="default line without the served record")
     ap.add_argument("--served-requests", type=int, default=100, help="requests per rate in the default line")
+    ap.add_argument("--max-batch", type=int, default=64, help="requests per served batch (--workload serve)")
+    ap.add_argument("--slots", type=int, default=4, help="streams of the render server (--workload serve)")
     return ap.parse_args()
 
 
@@ -526,6 +528,7 @@ def multiview_record(dev, steps, warmup, tile_shape=-1):
     b.check()
     samples_plain = int(r_vr.counters[0].item() + r_pj.counters[0].item()) // steps
     samples_batch = int(b.counters[0].item()) // steps
+    walks_batch = int(b.counters[1].item()) // steps
     same_images = all(torch.equal(pimg.view(torch.int64), j.image.view(torch.int64))
                       for (_, _, _, _, pimg, _, _), j in zip(prepared, jobs))
     ms_plain, ms_batch = np.array(ms_plain), np.array(ms_batch)
@@ -554,6 +557,7 @@ def multiview_record(dev, steps, warmup, tile_shape=-1):
                                      "p99": float(np.percentile(ms_plain, 99))},
                       "launches": len(jobs), "roofline_frac": gbs(ms_plain) / hbm},
             "samples_per_step": samples_batch, "samples_match": samples_batch == samples_plain,
+            "brick_walks_per_step": walks_batch,
             "images_identical_to_plain": bool(same_images),
             "launches_per_graph": len(b.groups), "work_items": b.total_tiles, "tile_shape": b.tile_shape,
             "roofline": {"bound": "hbm", "achieved": gbs(ms_batch), "peak": hbm, "unit": "GB/s",
@@ -774,7 +778,7 @@ def serve_requests(vols, n, rate, seed):
     return out
 
 
-def serve_record(dev, n_requests, rates, audit=None, amr=None):
+def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slots=4):
     """Served rendering against plain: at each rate the same Poisson stream
     goes through the render server (HBM-budget admission, continuous
     batching on four streams) and through the plain form (one single-view
@@ -786,7 +790,7 @@ def serve_record(dev, n_requests, rates, audit=None, amr=None):
     from yt_gb300.serve import RenderServer, latency_summary
 
     vols, tfs, t_build = serve_volumes(dev, amr)
-    srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=4, max_batch=64)
+    srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=slots, max_batch=max_batch)
     plain_srv = RenderServer({}, {}, device=dev, hbm_budget=16 << 30, plain=True)
     plain_srv.volumes, plain_srv.tfs = srv.volumes, srv.tfs
     # warm-up: compile paths, stage tables
@@ -842,7 +846,7 @@ def serve_record(dev, n_requests, rates, audit=None, amr=None):
             "audit": {"n": len(errs), "max_rel_err": float(max(errs)) if errs else None,
                       "vs": "float64 oracle", "sample": "every 100th served request"
                       + (f", {audit} of them spread evenly" if audit is not None else "")},
-            "requests_per_rate": n_requests, "slots": 4, "max_batch": 64, "hbm_budget_gib": 16,
+            "requests_per_rate": n_requests, "slots": slots, "max_batch": max_batch, "hbm_budget_gib": 16,
             "plain": "the same requests, one render_kernel launch each, one stream, in arrival order",
             "clocks": clocks.summary(), "build_seconds": t_build}
 
@@ -852,7 +856,7 @@ def run_serve(args):
 
     dev = torch.device("cuda", 0)
     rates = [float(x) for x in args.rates.split(",")]
-    rec = serve_record(dev, args.n_requests, rates, audit=args.audit)
+    rec = serve_record(dev, args.n_requests, rates, audit=args.audit, max_batch=args.max_batch, slots=args.slots)
     line = {"metric": "Gsamples/s & p50/p99 latency", "workload": "serve", "value": rec["value"],
             "unit": "Gsamples/s", "n_gpus": 1, "higher_is_better": True, "served": rec}
     print(json.dumps(line), flush=True)

@@ -215,15 +215,20 @@ int ytgb_trace(const ytgb_render_args *args, unsigned long long *hashes, long lo
 /* ---- device: many views in one persistent launch ------------------------- */
 /* Host: validate a batch (host copy of the entries; all of one sampler kind
  * and table layout) and number its tiles for a tile shape.  Writes
- * tile_begin / tiles_y / tiles of each entry, the total work items and the
- * shared memory the launch needs.  The same render as calling ytgb_render
- * for every entry; there is no reference counterpart (yt renders one
- * camera at a time). */
+ * tile_begin / tiles_y / tiles of each entry, the total tiles and the
+ * shared memory the launch stages its transfer function in: nonzero only
+ * when every entry reads the same tables (same pointer and header); 0 when
+ * they differ, and then the launch reads the tables from global memory.
+ * The same render as calling ytgb_render for every entry; there is no
+ * reference counterpart (yt renders one camera at a time). */
 int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t tile_shape, int32_t *total_tiles,
                     int32_t *smem_bytes);
 /* Device: render a planned batch (entries copied to device memory) with one
- * persistent launch of `blocks` blocks (<= 0: one wave of the GPU) pulling
- * work items from *d_queue, which it resets first.  Graph-capturable. */
+ * persistent launch of `blocks` blocks (<= 0: one wave of the GPU) whose
+ * warps pull 32-pixel work items from *d_queue, which it resets first.
+ * smem_bytes as ytgb_batch_plan wrote it (a staged table too large for it
+ * raises YTGB_DEVERR_BAD_TF in the error word instead of rendering).
+ * Graph-capturable. */
 int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t ctf_fast,
                       int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                       int32_t blocks, void *stream);

@@ -87,3 +87,16 @@ def test_noalloc_rejects_invalid_entry_arguments():
     entries[2].args.image = None
     st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
     assert st == _lib.ERR_INVALID and "missing image" in msg
+
+
+def test_plan_asks_for_shared_memory_only_for_one_shared_table():
+    """Entries that read different transfer functions are planned for the
+    global-memory table path (smem_bytes 0); staging one shared table
+    (smem_bytes > 0) is then rejected by the no-alloc entry point."""
+    entries, n, total, smem, ctf = planned()
+    entries[1].args.tf_tables = FAKE + 4096
+    t, sm = C.c_int32(), C.c_int32()
+    assert _lib.lib().ytgb_batch_plan(entries, n, 1, C.byref(t), C.byref(sm)) == _lib.OK
+    assert sm.value == 0 and t.value == total
+    st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
+    assert st == _lib.ERR_INVALID and "different" in msg

@@ -136,3 +136,31 @@ def test_batch_rejects_mixed_layouts():
 
     t, s = C.c_int32(), C.c_int32()
     assert _lib.lib().ytgb_batch_plan(e, 2, 0, C.byref(t), C.byref(s)) != 0
+
+
+def test_batch_views_with_different_tables(cuda):
+    """Views of one sampler class that read different transfer functions:
+    the plan asks for no shared memory and the batch reads each view's
+    tables from global memory; every image equals the view rendered alone
+    (which stages its tables in shared memory), bit for bit, and the
+    same views under one shared table take the staged path."""
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=32)
+    lg = [float(np.nanmin(b[0][0])) for b in w.bricks] + [float(np.nanmax(b[0][0])) for b in w.bricks]
+    lo, hi = min(lg), max(lg)
+    r_a = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
+    r_b = Renderer(r_a.bricks, workloads.color_tf((lo + 0.1, hi - 0.1), 5), device=cuda, kdtree=w.kdtree)
+    r_c = Renderer(r_a.bricks, workloads.color_tf((lo, hi), 3, nbins=128), device=cuda, kdtree=w.kdtree)
+    views = cams(6, seed=5)
+    mixed = Batch([Job([r_a, r_b, r_c][k % 3], cam, _lib.VOLUME_RENDER) for k, cam in enumerate(views)],
+                  device=cuda)
+    assert len(mixed.groups) == 1 and mixed.groups[0].smem == 0
+    shared = Batch([Job(r_b, cam, _lib.VOLUME_RENDER) for cam in views], device=cuda)
+    assert shared.groups[0].smem > 0
+    for b in (mixed, shared):
+        b.launch()
+        torch.cuda.synchronize()
+        b.check()
+        for j in b.jobs:
+            alone = j.renderer.render(j.camera, kind=j.kind)
+            assert float(alone.abs().max()) > 0
+            assert same_bits(alone, j.image)

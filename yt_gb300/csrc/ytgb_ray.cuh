@@ -47,6 +47,7 @@ YTGB_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
 YTGB_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
 YTGB_HD float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 YTGB_HD float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+YTGB_HD float frcp(float a) { return __frcp_rn(a); }
 YTGB_HD long long dbits(double x) { return __double_as_longlong(x); }
 template <typename T> YTGB_HD T ldg(const T *p) { return __ldg(p); }
 YTGB_HD bool finitef(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
@@ -63,6 +64,7 @@ YTGB_HD float fsub(float a, float b) { return a - b; }
 YTGB_HD float fmul(float a, float b) { return a * b; }
 YTGB_HD float ffma(float a, float b, float c) { return std::fmaf(a, b, c); }
 YTGB_HD float fdiv(float a, float b) { return a / b; }
+YTGB_HD float frcp(float a) { return 1.0f / a; }
 YTGB_HD long long dbits(double x) {
     long long b;
     std::memcpy(&b, &x, sizeof(b));
@@ -986,7 +988,8 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
         const int off = c0 * c.sx + c1 * c.sy + c2;
         if (MODE == MODE_VR && CTF) {
             const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
-            const bool in = !(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val);
+            // (NaN and infinities fail the strict bound tests, so they need no separate test)
+            const bool in = val < tf.hi_excl[0] && val > tf.lo_excl[0] && val != 0.0f;
             float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
             q = fminf(fmaxf(q, 0.0f), nbm2);  // a NaN q gives bin 0 (the sample is then out of range)
             const int bin = (int)q;
@@ -1103,7 +1106,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     // and 1e-4 of the operands' scale)
     float ifd[3];
     YTGB_UNROLL
-    for (int i = 0; i < 3; i++) ifd[i] = 1.0f / r.fdir[i];
+    for (int i = 0; i < 3; i++) ifd[i] = frcp(r.fdir[i]);  // = 1.0f / fdir, correctly rounded
     if (surely_misses(bf, r, ifd, st.max_tf)) return;
     const double max_t = st.max_t;
     const long long kmax = dkey(st.max_t);

@@ -44,6 +44,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -212,14 +213,32 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_re
 // warp's 32 pixels of a (view, tile) -- from a device counter until the
 // batch is drained, so small and large views share the GPU without a launch
 // per view and no warp waits for another.  An item's view is found by binary
-// search over the entries' first tiles.  Views may use different transfer
-// functions, so the tables are read from global memory (cached), not staged.
-// Every loop iteration takes a new item: a warp runs at most as many
-// iterations as there are items (no spin, no barrier).
-template <int MODE, int CTF, int TS>
+// search over the entries' first tiles.  STAGED: every entry uses the same
+// transfer-function tables (ytgb_batch_plan asks for shared memory only
+// then), staged once per block like render_kernel's; otherwise the views may
+// use different tables and read them from global memory (cached).  Every
+// loop iteration takes a new item: a warp runs at most as many iterations as
+// there are items (no spin, and no barrier after the staging).
+template <int MODE, int CTF, int TS, bool STAGED>
 __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
                                                       int total_tiles, int *queue) {
+    extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;
+    if (STAGED) {
+        // the launch's dynamic shared memory must hold the tables (a device
+        // table cannot be checked on the host): too little is an error, not
+        // a write out of bounds
+        unsigned dyn = 0;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        const ytgb_render_args &a0 = entries[0].args;
+        const size_t need = (size_t)(CTF ? 3 : a0.tf.n_fits) * a0.tf.nbins_max * sizeof(float4);
+        if (need > dyn) {
+            if (threadIdx.x == 0) set_error(a0.error, YTGB_DEVERR_BAD_TF);
+            return;
+        }
+        stage_tf<CTF>(a0, s_tab);
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const long long total_items = (long long)total_tiles * NWARP;
     while (true) {
@@ -237,9 +256,9 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_bat
         const ytgb_batch_entry &e = entries[lo];
         const int t = tile - __ldg(&e.tile_begin);
         const int ty = __ldg(&e.tiles_y);
-        warp_tile<MODE, CTF, TS, true>(e.args, t / ty, t % ty, item % NWARP,
-                                       reinterpret_cast<const float4 *>(e.args.tf_tables), sm, threadIdx.x, wl,
-                                       nullptr, nullptr);
+        const float4 *tab = STAGED ? s_tab : reinterpret_cast<const float4 *>(e.args.tf_tables);
+        warp_tile<MODE, CTF, TS, !STAGED>(e.args, t / ty, t % ty, item % NWARP, tab, sm, threadIdx.x, wl, nullptr,
+                                         nullptr);
     }
 }
 
@@ -297,6 +316,12 @@ int check_args(const ytgb_render_args *a, bool trace) {
         return YTGB_ERR_INVALID;
     }
     return YTGB_OK;
+}
+
+// Whether two launches read the same transfer function: the same packed
+// tables and an identical header.
+bool same_tf(const ytgb_render_args &a, const ytgb_render_args &b) {
+    return a.tf_tables == b.tf_tables && std::memcmp(&a.tf, &b.tf, sizeof(ytgb_tf)) == 0;
 }
 
 // Transfer-function header checks and the shared-memory bytes its tables take
@@ -378,19 +403,24 @@ int launch_ts(int ts, const ytgb_render_args *a, size_t smem, cudaStream_t s, un
 int tile_shape_of(uint32_t flags) { return (int)((flags >> YTGB_FLAG_TILE_SHIFT) & 0xfu); }
 
 template <int MODE, int CTF, int TS>
-int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t, cudaStream_t s) {
-    // the batch reads its transfer functions from global memory: no dynamic
-    // shared memory (the planned smem_bytes is what render_kernel stages)
+int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem,
+                   cudaStream_t s) {
+    // smem > 0: every entry shares the transfer function (ytgb_batch_plan),
+    // staged in shared memory; 0: tables read from global memory
+    const bool staged = smem > 0 && (MODE == MODE_VR || MODE == MODE_LIGHT);
+    auto kernel = staged ? batch_kernel<MODE, CTF, TS, true> : batch_kernel<MODE, CTF, TS, false>;
+    if (!staged) smem = 0;
+    if (int st = set_smem(kernel, smem)) return st;
     if (blocks <= 0) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, CTF, TS>, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem);
         blocks = sms * (per_sm > 0 ? per_sm : 1);
     }
     if (blocks > total) blocks = total;
     if (blocks < 1) blocks = 1;
-    batch_kernel<MODE, CTF, TS><<<blocks, BLOCK, 0, s>>>(d, n, total, queue);
+    kernel<<<blocks, BLOCK, smem, s>>>(d, n, total, queue);
     return launch_status("batch launch");
 }
 
@@ -455,6 +485,7 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
     const int ctf = kind == YTGB_VOLUME_RENDER ? entries[0].args.tf.ctf_fast : 0;
     long long total = 0;
     size_t smem = 0;
+    bool shared_tf = true;
     for (int32_t k = 0; k < n; k++) {
         ytgb_render_args &a = entries[k].args;
         if (int st = check_args(&a, false)) return st;
@@ -462,6 +493,7 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
             ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler and table layout");
             return YTGB_ERR_INVALID;
         }
+        shared_tf = shared_tf && same_tf(a, entries[0].args);
         if (kind == YTGB_VOLUME_RENDER || kind == YTGB_LIGHT_SOURCE) {
             size_t sm = 0;
             if (int st = tf_check(a.tf, &sm, kind == YTGB_VOLUME_RENDER && ctf != 0)) return st;
@@ -478,7 +510,7 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
         }
     }
     *total_tiles = (int32_t)total;
-    *smem_bytes = (int32_t)smem;
+    *smem_bytes = shared_tf ? (int32_t)smem : 0;
     return YTGB_OK;
 }
 
@@ -589,8 +621,10 @@ int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32
     const int TY = BLOCK / TX;
     long long total = 0;
     size_t smem = 0;
+    bool shared_tf = true;
     for (int32_t k = 0; k < n; k++) {
         const ytgb_render_args &a = h[k].args;
+        shared_tf = shared_tf && same_tf(a, h[0].args);
         if (int st = check_args(&a, false)) return st;
         if (a.kind != kind || (kind == YTGB_VOLUME_RENDER && (a.tf.ctf_fast != 0) != (ctf_fast != 0))) {
             ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
@@ -614,8 +648,11 @@ int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32
         ytgb_set_error("ytgb_batch_render_noalloc: total_tiles does not match the planned entries");
         return YTGB_ERR_INVALID;
     }
-    if ((size_t)smem_bytes < smem) {
-        ytgb_set_error("ytgb_batch_render_noalloc: smem_bytes is below what the entries' tables take");
+    if (smem_bytes > 0 && (kind == YTGB_VOLUME_RENDER || kind == YTGB_LIGHT_SOURCE) &&
+        (!shared_tf || (size_t)smem_bytes < smem)) {
+        ytgb_set_error(shared_tf ? "ytgb_batch_render_noalloc: smem_bytes is below what the entries' tables take"
+                                 : "ytgb_batch_render_noalloc: smem_bytes > 0 stages one transfer function, but "
+                                   "the entries use different ones");
         return YTGB_ERR_INVALID;
     }
     return YTGB_OK;

@@ -7,11 +7,11 @@ over time.  The loop:
 * **admits** arrived requests while their output images fit the HBM budget
   (a request waits in the arrival queue otherwise);
 * **batches** every admitted, not yet launched request into one
-  :class:`~yt_gb300.batch.Batch` (one persistent launch per sampler class)
-  as soon as one of ``slots`` CUDA streams is free -- so requests that arrive
-  while earlier batches are on the GPU start on another stream at once and
-  their work overlaps on the device (continuous batching, not a queue in
-  front of one stream);
+  :class:`~yt_gb300.batch.Batch` (one persistent launch per sampler class;
+  a lone request takes the single-view kernel) as soon as one of ``slots``
+  CUDA streams is free -- so requests that arrive while earlier batches are
+  on the GPU start on another stream at once and their work overlaps on the
+  device (continuous batching, not a queue in front of one stream);
 * **retires** a batch when its completion event fires, frees its images'
   budget and records each request's latency (completion - arrival);
 * **drops** requests cancelled before their launch (``Request.cancelled``),
@@ -55,6 +55,7 @@ class Request:
     image: torch.Tensor | None = None
     samples: int = 0
     cancelled: bool = False       # set before launch: the request is dropped, never rendered
+    batch_size: int = 0           # requests in the launch that rendered it
 
     @property
     def image_bytes(self) -> int:
@@ -127,7 +128,12 @@ class RenderServer:
         return r
 
     def _launch(self, reqs, stream, now):
-        if self.plain:
+        # a batch of one renders through the single-view kernel (which
+        # stages its table in shared memory and needs no work queue); the
+        # persistent batch kernel pays off from two views on
+        for q in reqs:
+            q.batch_size = len(reqs)
+        if self.plain or len(reqs) == 1:
             return self._launch_plain(reqs, stream, now)
         jobs = []
         for q in reqs:
