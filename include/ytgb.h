@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define YTGB_ABI_VERSION 3
+#define YTGB_ABI_VERSION 4
 
 #define YTGB_OK 0
 #define YTGB_ERR_INVALID (-1)   /* bad argument, detected on the host */
@@ -128,6 +128,9 @@ typedef struct ytgb_tf {
     float hi_excl[6];   /* smallest float >= bounds[1]: v >= hi_excl -> 0 */
     float b0[6];        /* bounds[0] as float, for the bin index */
     float idbin[6];     /* 1/dbin as float, for the bin index */
+    double bound64[6][2]; /* the bounds as given: a sample whose float32 value lies
+                           * within its rounding error of a bound (or of 0) is
+                           * decided in float64, as FIT_get_value does */
     /* table floats follow in a separate buffer: for table t, bin b:
      * tab[(t*nbins_max + b)*4 + {0,1,2,3}] = {y, dy, d0_hi, d0_lo} */
 } ytgb_tf;
@@ -156,12 +159,19 @@ typedef struct ytgb_render_args {
     unsigned long long *counters; /* device [4]: cell visits, ray-brick walks, rays, cells
                                   * outside their brick (skipped); or NULL */
     int32_t *error;            /* device error word (0 = ok), or NULL */
+    const float *data_lo;      /* device: data - (float)data for every arena value, or
+                                * NULL (taken as 0): the light-source gradient's
+                                * differences, and the range decisions below */
     /* LightSourceRenderSampler only (image_samplers.pyx:496-590) */
-    const float *data_lo;      /* device: data - (float)data for every arena value (the
-                                * gradient's differences), or NULL (taken as 0) */
     float light_dir[3];        /* normalised light direction */
     float light_rgba[4];
-    int32_t pad_light;
+    /* Volume rendering and light source with data_lo: M * 2^-24, M >= every
+     * |value| of the arena.  A sample whose float32 value is 0 or lies within
+     * range_eps * (96 + 16 * (dims0 + dims1 + dims2 + 3)) of a transfer-function
+     * bound (its float32 error bound, twice over) is decided as FIT_get_value
+     * decides it (field_interpolation_tables.pxd:66-80): from yt's float64
+     * value, recomputed from data + data_lo.  0: float32 decisions only. */
+    float range_eps;
 } ytgb_render_args;
 
 /* One view of a multi-view batch (device memory), as filled by
@@ -214,7 +224,8 @@ int ytgb_trace(const ytgb_render_args *args, unsigned long long *hashes, long lo
 
 /* ---- device: many views in one persistent launch ------------------------- */
 /* Host: validate a batch (host copy of the entries; all of one sampler kind
- * and table layout) and number its tiles for a tile shape.  Writes
+ * and kernel variant, YTGB_VARIANT_* below) and number its tiles for a tile
+ * shape.  Writes
  * tile_begin / tiles_y / tiles of each entry, the total tiles and the
  * shared memory the launch stages its transfer function in: nonzero only
  * when every entry reads the same tables (same pointer and header); 0 when
@@ -223,13 +234,21 @@ int ytgb_trace(const ytgb_render_args *args, unsigned long long *hashes, long lo
  * reference counterpart (yt renders one camera at a time). */
 int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t tile_shape, int32_t *total_tiles,
                     int32_t *smem_bytes);
+/* The kernel variant of a batch (ytgb_batch_plan requires every entry to
+ * call for the same one): YTGB_VARIANT_CTF where the volume-rendering tables
+ * are a ColorTransferFunction (tf.ctf_fast), plus YTGB_VARIANT_RANGE64
+ * where volume-rendering or light-source entries carry data_lo and
+ * range_eps > 0 (float64 range decisions near a bound; not for a
+ * ColorTransferFunction whose table excludes every value). */
+#define YTGB_VARIANT_CTF 1
+#define YTGB_VARIANT_RANGE64 2
 /* Device: render a planned batch (entries copied to device memory) with one
  * persistent launch of `blocks` blocks (<= 0: one wave of the GPU) whose
  * warps pull 32-pixel work items from *d_queue, which it resets first.
  * smem_bytes as ytgb_batch_plan wrote it (a staged table too large for it
  * raises YTGB_DEVERR_BAD_TF in the error word instead of rendering).
- * Graph-capturable. */
-int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+ * variant: the entries' YTGB_VARIANT_* bits.  Graph-capturable. */
+int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t variant,
                       int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                       int32_t blocks, void *stream);
 
@@ -239,7 +258,7 @@ int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind
  * counter, then the persistent launch runs from there.  No counterpart in
  * the reference (yt renders one camera at a time and allocates per call).
  * The host table is checked against the arguments before anything is
- * queued (each entry's arguments, sampler kind and table layout, smem_bytes
+ * queued (each entry's arguments, sampler kind and variant, smem_bytes
  * against the entries' tables, the tile numbering ytgb_batch_plan writes for
  * tile_shape, total_tiles); a mismatch returns YTGB_ERR_INVALID.
  * Limits: at most YTGB_NOALLOC_MAX_ENTRIES views per call (more is rejected
@@ -254,7 +273,7 @@ int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind
  * the stream has passed the call.  The counter is cleared by every call;
  * nothing needs to be zero beforehand. */
 #define YTGB_NOALLOC_MAX_ENTRIES 128
-int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind, int32_t variant,
                               int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t blocks,
                               void *stream);
 

@@ -12,13 +12,13 @@
 #include "ytgb_octree.cuh"
 using namespace ytgb;
 
-template <int MODE, int CTF>
+template <int MODE, int VAR>
 static void run(const ytgb_render_args &a, unsigned long long *hashes, long long *counts, unsigned long long *cnt) {
     std::vector<float4> tab;
     if (MODE == MODE_VR || MODE == MODE_LIGHT) {
         const float4 *g = reinterpret_cast<const float4 *>(a.tf_tables);
         int nb = a.tf.nbins_max;
-        if (CTF) {
+        if (VAR & V_CTF) {
             tab.resize(3 * nb);
             for (int b = 0; b < nb; b++) {
                 float4 t0 = g[b], t1 = g[nb + b], t2 = g[2 * nb + b], t3 = g[3 * nb + b];
@@ -43,7 +43,7 @@ static void run(const ytgb_render_args &a, unsigned long long *hashes, long long
             for (int k = 0; k < a.n_order; k++) {
                 int4 rc = rects[k];
                 if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
-                walk_brick<MODE, CTF>(a, tab.data(), r, a.order[k], st);
+                walk_brick<MODE, VAR>(a, tab.data(), r, a.order[k], st);
             }
             if (MODE == MODE_TRACE) { hashes[p] = st.th; counts[p] = st.tcount; }
             else for (int c = 0; c < 4; c++) if (st.touched & (1u << c)) img[c] = (double)st.xh[c] + (double)st.xl[c];
@@ -55,10 +55,20 @@ extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long lo
                           unsigned long long *cnt) {
     if (trace) { run<MODE_TRACE, 0>(*a, hashes, counts, cnt); return 0; }
     switch (a->kind) {
-    case YTGB_VOLUME_RENDER: if (a->tf.ctf_fast) run<MODE_VR, 1>(*a, 0, 0, cnt); else run<MODE_VR, 0>(*a, 0, 0, cnt); break;
+    case YTGB_VOLUME_RENDER:
+        switch (render_variant(*a)) {
+        case V_CTF: run<MODE_VR, V_CTF>(*a, 0, 0, cnt); break;
+        case V_REF: run<MODE_VR, V_REF>(*a, 0, 0, cnt); break;
+        case V_CTF | V_REF: run<MODE_VR, V_CTF | V_REF>(*a, 0, 0, cnt); break;
+        default: run<MODE_VR, 0>(*a, 0, 0, cnt);
+        }
+        break;
     case YTGB_PROJECTION: run<MODE_PROJ, 0>(*a, 0, 0, cnt); break;
     case YTGB_INTERPOLATED_PROJECTION: run<MODE_IPROJ, 0>(*a, 0, 0, cnt); break;
-    case YTGB_LIGHT_SOURCE: run<MODE_LIGHT, 0>(*a, 0, 0, cnt); break;
+    case YTGB_LIGHT_SOURCE:
+        if (render_variant(*a) & V_REF) run<MODE_LIGHT, V_REF>(*a, 0, 0, cnt);
+        else run<MODE_LIGHT, 0>(*a, 0, 0, cnt);
+        break;
     default: run<MODE_MIP, 0>(*a, 0, 0, cnt);
     }
     return 0;

@@ -62,7 +62,30 @@ def test_noalloc_rejects_mismatched_kind_and_layout():
     st, msg = noalloc(entries, n, _lib.PROJECTION, 0, 1, total, 0)
     assert st == _lib.ERR_INVALID and "sampler kind" in msg
     st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, 0, 1, total, smem)
-    assert st == _lib.ERR_INVALID and "table layout" in msg
+    assert st == _lib.ERR_INVALID and "variant" in msg
+
+
+def test_range_decisions_are_one_variant():
+    """Entries with the arena's rounding errors (data_lo, range_eps > 0) take
+    the float64 range-decision kernels: a batch may not mix them with
+    entries without, and the launch's variant must say which."""
+    entries, n, total, smem, ctf = planned()
+    entries[0].args.data_lo = FAKE
+    entries[0].args.range_eps = 1e-7
+    L = _lib.lib()
+    t, sm = C.c_int32(), C.c_int32()
+    assert L.ytgb_batch_plan(entries, n, 1, C.byref(t), C.byref(sm)) == _lib.ERR_INVALID
+    assert "range decisions" in L.ytgb_last_error().decode()
+    for k in range(n):
+        entries[k].args.data_lo = FAKE
+        entries[k].args.range_eps = 1e-7
+    assert L.ytgb_batch_plan(entries, n, 1, C.byref(t), C.byref(sm)) == _lib.OK
+    assert _lib.render_variant(entries[0].args) == _lib.VARIANT_CTF | _lib.VARIANT_RANGE64
+    st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
+    assert st == _lib.ERR_INVALID and "variant" in msg
+    entries[1].args.range_eps = float("nan")
+    assert L.ytgb_batch_plan(entries, n, 1, C.byref(t), C.byref(sm)) == _lib.ERR_INVALID
+    assert "range_eps" in L.ytgb_last_error().decode()
 
 
 def test_noalloc_rejects_short_shared_memory():

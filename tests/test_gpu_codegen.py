@@ -79,7 +79,7 @@ def test_other_register_budget_same_images(cuda, variant):
         im.zero_()
     stream = torch.cuda.current_stream(cuda)
     for q, g in enumerate(b.groups):
-        st = variant.ytgb_batch_render(g.dev.data_ptr(), g.n, g.kind, g.ctf, b.tile_shape, g.total_tiles, g.smem,
+        st = variant.ytgb_batch_render(g.dev.data_ptr(), g.n, g.kind, g.variant, b.tile_shape, g.total_tiles, g.smem,
                                        b.queue.data_ptr() + 4 * q, 0, C.c_void_p(stream.cuda_stream))
         assert st == _lib.OK, variant.ytgb_last_error()
     torch.cuda.synchronize()

@@ -23,7 +23,7 @@ from yt_gb300.image_samplers import make_view
 from yt_gb300.render import relative_error
 from yt_gb300.transfer_functions import (ColorTransferFunction, MultiVariateTransferFunction, TransferFunction,
                                          pack)
-from yt_gb300.volume import BrickSet, set_light
+from yt_gb300.volume import BrickSet, set_light, set_range
 
 ROOT = Path(__file__).resolve().parent.parent
 HERE = Path(__file__).resolve().parent / "kernel_host"
@@ -53,8 +53,12 @@ def emu():
     return L
 
 
-def run_emu(L, bricks, cam, order, kind, tf=None, ns=1, zbuffer=None, light=None, with_lo=True):
-    bs = BrickSet(bricks, device="cpu", with_lo=(kind == _lib.LIGHT_SOURCE and with_lo))
+def run_emu(L, bricks, cam, order, kind, tf=None, ns=1, zbuffer=None, light=None, with_lo=None):
+    """with_lo: the arena's float32 rounding errors (None: for the light
+    source, whose gradient uses them; True also takes the float64 range
+    decisions of volume rendering and the light source)."""
+    lo = (kind == _lib.LIGHT_SOURCE) if with_lo is None else bool(with_lo)
+    bs = BrickSet(bricks, device="cpu", with_lo=lo)
     p = cam.sampler_params()
     nx, ny = cam.resolution
     view, ppos, pdir = make_view(p["vp_pos"], p["vp_dir"], p["center"], p["bounds"], nx, ny, p["x_vec"],
@@ -79,6 +83,8 @@ def run_emu(L, bricks, cam, order, kind, tf=None, ns=1, zbuffer=None, light=None
         a.zbuffer = zbuffer.ctypes.data
     if kind == _lib.LIGHT_SOURCE:
         set_light(a, bs, light)
+    elif kind == _lib.VOLUME_RENDER:
+        set_range(a, bs)
     img = np.zeros((nx, ny, 4))
     a.image = img.ctypes.data
     cnt = np.zeros(4, dtype=np.uint64)
@@ -177,6 +183,65 @@ def test_grey_opacity_and_multivariate(emu):
     mv.add_field_table(t1, 0, weight_field_id=1, weight_table_id=0)
     mv.link_channels(1, [0, 1, 2])
     check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=mv)
+
+
+def near_bound_case(n=8, seed=3):
+    """One brick whose every vertex value lies within 1e-9 of b = 1 + 2^-30,
+    the upper bound of the transfer functions below: float32 has no value
+    between 1 and 1 + 2^-23, so every stored value is 1.0 and every float32
+    sample falls inside the range, while yt's float64 test drops the samples
+    at or above b -- about half (field_interpolation_tables.pxd:72-73)."""
+    rng = np.random.default_rng(seed)
+    b = 1.0 + 2.0 ** -30
+    v = b + rng.uniform(-1e-9, 1e-9, (n + 1,) * 3)
+    bricks = [([v], None, np.zeros(3), np.ones(3), np.array([n, n, n]))]
+    ctf = workloads.color_tf((b - 1.0, b), 4)
+    tf = TransferFunction((b - 1.0, b), 64)
+    tf.add_gaussian(b - 0.02, 0.01, 1.0)
+    mv = MultiVariateTransferFunction()
+    mv.add_field_table(tf, 0)
+    mv.link_channels(0, [0, 1, 2, 3])
+    return bricks, {"ctf": ctf, "general": mv}
+
+
+@pytest.mark.parametrize("which,kind,ns", [("ctf", _lib.VOLUME_RENDER, 1), ("ctf", _lib.VOLUME_RENDER, 3),
+                                           ("general", _lib.VOLUME_RENDER, 1),
+                                           ("ctf", _lib.LIGHT_SOURCE, 2)])
+def test_range_decisions_near_a_bound(emu, which, kind, ns):
+    """With the arena's rounding errors (data_lo) and their scale
+    (range_eps) the kernel decides every sample within its float32 error of
+    a bound from yt's float64 value, and matches the oracle; without them it
+    keeps every sample of this field and misses by far."""
+    bricks, tfs = near_bound_case()
+    tf = tfs[which]
+    cam = Camera((0.3, 0.6, -1.0), 0.5, 1.5, 24, lens_type="perspective")
+    order = np.array([0])
+    # (the light source with light_rgba 0: this field's gradient is rounding
+    # noise, which yt normalises into an arbitrary direction)
+    light = ((1.0, 1.0, 1.0), (0.0, 0.0, 0.0, 0.0)) if kind == _lib.LIGHT_SOURCE else None
+    ref, visits, *_ = run_oracle(bricks, cam, order, kind, tf, ns, light=light)
+    chans = (0, 1, 2)
+    img, cnt, *_ = run_emu(emu, bricks, cam, order, kind, tf, ns, light=light, with_lo=True)
+    assert relative_error(img, ref, channels=chans)[0] <= TOL and int(cnt[0]) == visits
+    if kind == _lib.VOLUME_RENDER:
+        f32, *_ = run_emu(emu, bricks, cam, order, kind, tf, ns, with_lo=False)
+        assert relative_error(f32, ref, channels=chans)[0] > 1e-2
+
+
+def test_range_decision_tolerance_covers_float32_error(emu):
+    """The tolerance (range_tol) bounds the float32 sample value's error:
+    on AMR bricks with a transfer function whose bounds cut through the
+    data, the float32 and the float64-decided renders differ only where a
+    sample lies within the tolerance of a bound, and the float64-decided
+    one matches the oracle."""
+    w = workloads.amr_vr(root=32, levels=2, patch=8, res=48)
+    cam = Camera((1.3, -0.4, 1.1), (0.5, 0.5, 0.5), 1.4, 48, lens_type="perspective")
+    order = w.order(cam)
+    for lo, hi in ((0.1, 0.9), (0.35, 1.25)):
+        tf = workloads.color_tf((lo, hi), 6)
+        ref, *_ = run_oracle(w.bricks, cam, order, _lib.VOLUME_RENDER, tf)
+        img, *_ = run_emu(emu, w.bricks, cam, order, _lib.VOLUME_RENDER, tf, with_lo=True)
+        assert relative_error(img, ref, channels=(0, 1, 2))[0] <= TOL
 
 
 def test_projection_transfer_function_bounds(emu):

@@ -59,7 +59,7 @@ def test_noalloc_matches_batch_render(cuda):
         for im in b.images:
             im.zero_()
         for g in b.groups:
-            st = L.ytgb_batch_render_noalloc(g.entries, g.n, g.kind, g.ctf, b.tile_shape, g.total_tiles, g.smem, 0,
+            st = L.ytgb_batch_render_noalloc(g.entries, g.n, g.kind, g.variant, b.tile_shape, g.total_tiles, g.smem, 0,
                                             C.c_void_p(stream.cuda_stream))
             _lib.check(st, "ytgb_batch_render_noalloc")
         torch.cuda.synchronize()

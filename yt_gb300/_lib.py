@@ -20,6 +20,7 @@ EXTENT_PLANE_PARALLEL, EXTENT_PERSPECTIVE, EXTENT_NULL = 0, 1, 2
 FLAG_NO_COMPENSATION = 1
 FLAG_TILE_SHIFT = 8
 NOALLOC_MAX_ENTRIES = 128  # YTGB_NOALLOC_MAX_ENTRIES
+VARIANT_CTF, VARIANT_RANGE64 = 1, 2  # YTGB_VARIANT_*
 FNV_OFFSET = 1469598103934665603
 
 _dp = C.POINTER(C.c_double)
@@ -82,6 +83,7 @@ class TF(C.Structure):
         ("hi_excl", C.c_float * 6),
         ("b0", C.c_float * 6),
         ("idbin", C.c_float * 6),
+        ("bound64", (C.c_double * 2) * 6),
     ]
 
 
@@ -107,7 +109,7 @@ class RenderArgs(C.Structure):
         ("data_lo", C.c_void_p),
         ("light_dir", C.c_float * 3),
         ("light_rgba", C.c_float * 4),
-        ("pad_light", C.c_int32),
+        ("range_eps", C.c_float),
     ]
 
 
@@ -236,10 +238,24 @@ def lib() -> C.CDLL:
                 fn = getattr(L, name)
                 fn.restype = res
                 fn.argtypes = args
-            if L.ytgb_abi_version() != 3:
+            if L.ytgb_abi_version() != 4:
                 raise YtgbError("libytgb ABI version mismatch")
             _lib = L
     return _lib
+
+
+def render_variant(a) -> int:
+    """The kernel variant (YTGB_VARIANT_* bits) a RenderArgs calls for: the
+    ColorTransferFunction layout, and float64 range decisions where the
+    arena's rounding errors (data_lo) and range_eps > 0 are given -- except
+    for a ColorTransferFunction whose table excludes every value."""
+    v = 0
+    if a.kind == VOLUME_RENDER and a.tf.ctf_fast:
+        v |= VARIANT_CTF
+    if (a.kind in (VOLUME_RENDER, LIGHT_SOURCE) and a.data_lo and a.range_eps > 0.0
+            and (not v & VARIANT_CTF or a.tf.lo_excl[0] <= a.tf.hi_excl[0])):
+        v |= VARIANT_RANGE64
+    return v
 
 
 def check(status: int, what: str) -> None:

@@ -188,6 +188,7 @@ class AMRKDTree:
                                         bs.data_lo.data_ptr() if bs.data_lo is not None else None),
                    "ytgb_vertex_bricks")
         _lib.check(L.ytgb_check_error(error.data_ptr(), s.cuda_stream), "ytgb_vertex_bricks")
+        bs.data_changed()
         self.device_upload_bytes = int(cells.numel() * 8 + meta_i64.numel() * 8 + meta_i32.numel() * 4 +
                                        bs.upload_bytes)
         return bs

@@ -23,7 +23,7 @@ import torch
 from . import _lib
 from .autotune import tile_shape_for
 from .render import Renderer
-from .volume import check_inputs, set_light
+from .volume import check_inputs, set_light, set_range
 
 
 @dataclass
@@ -41,7 +41,7 @@ class Job:
 @dataclass
 class _Group:
     kind: int
-    ctf: int
+    variant: int                    # YTGB_VARIANT_* bits
     entries: object = None          # ctypes array of BatchEntry
     dev: torch.Tensor | None = None  # the entries in device memory
     n: int = 0
@@ -97,8 +97,6 @@ class Batch:
             tf = j.renderer.packed if uses_tf else None
             if uses_tf and tf is None:
                 raise ValueError("volume rendering needs a transfer function")
-            ctf = int(tf.header.ctf_fast) if (tf is not None and j.kind == _lib.VOLUME_RENDER) else 0
-            g = groups.setdefault((j.kind, ctf), _Group(j.kind, ctf))
             a = _lib.RenderArgs()
             a.kind = j.kind
             a.n_samples = j.n_samples
@@ -117,9 +115,12 @@ class Batch:
             a.image = j.image.data_ptr()
             if j.kind == _lib.LIGHT_SOURCE:
                 set_light(a, j.renderer.bricks, j.light)
+            elif j.kind == _lib.VOLUME_RENDER:
+                set_range(a, j.renderer.bricks)
             a.counters = self.counters.data_ptr()
             a.error = self.error.data_ptr()
-            g.jobs.append(a)
+            var = _lib.render_variant(a)
+            groups.setdefault((j.kind, var), _Group(j.kind, var)).jobs.append(a)
         self.groups = list(groups.values())
         L = _lib.lib()
         for g in self.groups:
@@ -149,7 +150,7 @@ class Batch:
             for im in self.images:
                 im.zero_()
         for q, g in enumerate(self.groups):
-            _lib.check(L.ytgb_batch_render(g.dev.data_ptr(), g.n, g.kind, g.ctf, self.tile_shape, g.total_tiles,
+            _lib.check(L.ytgb_batch_render(g.dev.data_ptr(), g.n, g.kind, g.variant, self.tile_shape, g.total_tiles,
                                            g.smem, self.queue.data_ptr() + 4 * q, self.blocks,
                                            C.c_void_p(stream.cuda_stream)), "ytgb_batch_render")
 

@@ -353,6 +353,8 @@ extern "C" int ytgb_tf_pack(int32_t n_fits, const double *const *values, const i
         tf->hi_excl[t] = float_at_or_above(b1);
         tf->b0[t] = (float)b0;
         tf->idbin[t] = (float)idbin;
+        tf->bound64[t][0] = b0;
+        tf->bound64[t][1] = b1;
         // Bounds beyond float32's range (ProjectionTransferFunction uses
         // +-1e60, transfer_functions.py:946-960) leave no float32 form of the
         // bin arithmetic.  yt's float64 lookup of such a table returns

@@ -254,6 +254,9 @@ YTGB_HD bool octree_ray(const ytgb_render_args &a, const OctreeView &o, const fl
         c.nf = 1;
         c.sx = 4;
         c.sy = 2;
+        c.tol = -1.0f;  // octree cells: float32 range decisions
+        c.ray = nullptr;
+        c.bp = nullptr;
         float P[3];
         if (o.edges_f) {
             // (enter * v_dir + v_pos - left_edge) * idds (image_samplers.pyx:

@@ -553,6 +553,83 @@ YTGB_HD float trilinear(const float *__restrict__ p, int sy, int sx, float dx, f
     return ffma(dx, fsub(b1, b0), b0);
 }
 
+// yt's float64 value of a field at sample s (of ns) in a cell
+// (VolumeRenderSampler.sample, image_samplers.pyx:471-481, and
+// offset_interpolate, fixed_interpolator.cpp:34-52), from the walk's exact
+// enter/exit t, the ray, the brick's edges and cell widths, and the float64
+// vertex values as their float32 parts plus float32 rounding errors
+// (hi + lo is the float64 value to 2^-48).  Every operation is yt's, in
+// yt's order.
+YTGB_HD double yt_sample_value(const Ray &r, const ytgb_brick *bp, const float *__restrict__ hi,
+                               const float *__restrict__ lo, int sy, int sx, const int cur[3], long long eb,
+                               long long xb, int ns, int s) {
+    const double en = dfrom(eb), ex = dfrom(xb);
+    const double dt = ddiv(dsub(ex, en), (double)ns);
+    double dp[3];
+    YTGB_UNROLL
+    for (int i = 0; i < 3; i++) {
+        const double idds = ldg(&bp->idds[i]);
+        dp[i] = dadd(dmul(dadd(en, dmul(0.5, dt)), r.dir[i]), r.pos[i]);
+        dp[i] = dsub(dp[i], dadd(dmul((double)cur[i], ldg(&bp->dds[i])), ldg(&bp->left_edge[i])));
+        dp[i] = dmul(dp[i], idds);
+        const double ds = dmul(dmul(r.dir[i], idds), dt);
+        for (int k = 0; k < s; k++) dp[i] = dadd(dp[i], ds);
+    }
+    double c[8];
+    YTGB_UNROLL
+    for (int q = 0; q < 8; q++) {
+        const int o = ((q >> 2) & 1) * sx + ((q >> 1) & 1) * sy + (q & 1);
+        c[q] = dadd((double)ldg(hi + o), (double)ldg(lo + o));
+    }
+    double dv = dsub(1.0, dp[2]);
+    double v0 = dadd(dmul(dv, c[0]), dmul(dp[2], c[1]));
+    double v1 = dadd(dmul(dv, c[2]), dmul(dp[2], c[3]));
+    double v2 = dadd(dmul(dv, c[4]), dmul(dp[2], c[5]));
+    double v3 = dadd(dmul(dv, c[6]), dmul(dp[2], c[7]));
+    dv = dsub(1.0, dp[1]);
+    v0 = dadd(dmul(dv, v0), dmul(dp[1], v1));
+    v1 = dadd(dmul(dv, v2), dmul(dp[1], v3));
+    dv = dsub(1.0, dp[0]);
+    return dadd(dmul(dv, v0), dmul(dp[0], v1));
+}
+
+// FIT_get_value's range test in float64 (field_interpolation_tables.pxd:
+// 66-80): 0 outside the open interval of the bounds and for non-normal values.
+YTGB_HD bool fit_in_range64(double v, double b0, double b1) {
+    if (!(v < b1) || !(v > b0)) return false;  // also NaN
+    const long long e = (dbits(v) >> 52) & 0x7ff;
+    return e != 0 && e != 0x7ff;  // isnormal: not zero, subnormal, inf or NaN
+}
+
+// FIT_get_value's float64 range decision for a sample (yt_sample_value of
+// the field whose vertex values start at hi; lo: their rounding errors).
+YTGB_HD bool range_in64(const Ray *r, const ytgb_brick *bp, const float *hi, const float *lo, int sy, int sx,
+                             int c0, int c1, int c2, long long eb, long long xb, int ns, int s, double b0,
+                             double b1) {
+    const int cur[3] = {c0, c1, c2};
+    return fit_in_range64(yt_sample_value(*r, bp, hi, lo, sy, sx, cur, eb, xb, ns, s), b0, b1);
+}
+
+// The range decision's tolerance for a walk of at most `steps` cells:
+// twice the float32 error bound of a sample value.  With M >= every |value|
+// (eps = M 2^-24) the value's error against yt's float64 one is at most
+//   2^-24 M (the float32 vertex values) + 16 eps (the seven interpolation
+//   roundings and their differences) + 3 * 2M * dx,
+// dx being the cell-coordinate error: <= (steps / 2 + 4) 2^-24, from the
+// float32 entry point, dt and velocity and one half-ulp ffma rounding per
+// step since the axis last snapped to a face (advance_position).  Hence
+// 41 + 6 steps, doubled.
+YTGB_HD float range_tol(float eps, int steps) { return fmul(eps, (float)(96 + 16 * steps)); }
+
+// Whether FIT_get_value's float64 range test (field_interpolation_tables.pxd:
+// 72-73) could decide a sample differently from the float32 test on its
+// float32 value v: v within tol of a bound, or v exactly 0 (yt's isnormal
+// test; a float64 value that is exactly 0 where v is not needs an exact
+// float64 cancellation that float32 does not reproduce).
+YTGB_HD bool range_ambiguous(float v, float tol, float lo, float hi) {
+    return v == 0.0f || fabsf(fsub(v, lo)) <= tol || fabsf(fsub(v, hi)) <= tol;
+}
+
 // eval_gradient (fixed_interpolator.cpp:116-148) of the trilinear
 // interpolant in cell coordinates, normalised to -grad/|grad| (0 when the
 // gradient vanishes).  The reference takes finite differences 0.05 apart
@@ -627,14 +704,18 @@ YTGB_HD void ctf_bin(const float4 *__restrict__ tab, int nbins, int bin, float4 
 // float64 test would for that v.  Zero, infinite and NaN values give 0 like
 // the reference's !isnormal test.
 YTGB_HD void tf_eval(const ytgb_tf &tf, const float4 *__restrict__ tab, const float dvs[6],
-                                        float trgba[6]) {
+                                        float trgba[6], unsigned force = 0u, unsigned force_in = 0u) {
     float ist[6];
     YTGB_UNROLL
     for (int t = 0; t < 6; t++) {
         ist[t] = 0.0f;
         if (t < tf.n_fits) {
             float v = pick6(dvs, tf.field_id[t]);
-            if (!(v >= tf.hi_excl[t] || v <= tf.lo_excl[t]) && v != 0.0f && finitef(v)) {
+            // (force: table t's range decision taken from bit t of force_in)
+            const bool in = (force >> t) & 1u ? ((force_in >> t) & 1u) != 0u
+                                              : !(v >= tf.hi_excl[t] || v <= tf.lo_excl[t]) && v != 0.0f &&
+                                                    finitef(v);
+            if (in) {
                 float q = fmul(fsub(v, tf.b0[t]), tf.idbin[t]);
                 q = fminf(fmaxf(q, 0.0f), (float)(tf.nbins[t] - 2));
                 int bin = (int)q;
@@ -714,7 +795,55 @@ struct CellCtx {
     int nf, sx, sy;
     int dims[3];
     float vel[3];
+    // the float64 range decision (range_ambiguous): its tolerance, < 0 for
+    // float32 decisions only, and the ray and brick it recomputes from
+    float tol;
+    const Ray *ray;
+    const ytgb_brick *bp;
 };
+
+// The sampler variant, a template parameter (VAR) of the volume-rendering
+// and light-source paths: bit V_CTF, the ColorTransferFunction layout
+// (ctf_bin); bit V_REF, range decisions near a bound made in float64 from
+// data + data_lo (range_ambiguous, set where the launch carries data_lo and
+// range_eps > 0).
+constexpr int V_CTF = 1;
+constexpr int V_REF = 2;
+
+// The variant a render's arguments call for: float64 range decisions where
+// the arena's rounding errors and their scale are given, except for a
+// ColorTransferFunction whose table excludes every value (nothing is in
+// range either way).
+inline int render_variant(const ytgb_render_args &a) {
+    int v = 0;
+    if (a.kind == YTGB_VOLUME_RENDER && a.tf.ctf_fast) v |= V_CTF;
+    if ((a.kind == YTGB_VOLUME_RENDER || a.kind == YTGB_LIGHT_SOURCE) && a.data_lo && a.range_eps > 0.0f &&
+        (!(v & V_CTF) || a.tf.lo_excl[0] <= a.tf.hi_excl[0]))
+        v |= V_REF;
+    return v;
+}
+
+// The tables of a general transfer function whose range decision for the
+// field values dvs is made in float64 (range_ambiguous): bit t of force, and
+// of force_in where yt's float64 value lies inside table t's range.
+YTGB_HD void range_decisions(const ytgb_render_args &a, const CellCtx &c, const float dvs[6], int off,
+                             const int cur[3], long long eb, long long xb, int ns, int s, unsigned &force,
+                             unsigned &force_in) {
+    force = 0u;
+    force_in = 0u;
+    if (c.tol < 0.0f) return;
+    const ytgb_tf &tf = a.tf;
+    for (int t = 0; t < tf.n_fits; t++) {
+        const int f = tf.field_id[t];
+        if (f >= c.nf || !(tf.lo_excl[t] <= tf.hi_excl[t])) continue;
+        if (!range_ambiguous(pick6(dvs, f), c.tol, tf.lo_excl[t], tf.hi_excl[t])) continue;
+        const float *hi = c.base + f * c.fstride + off;
+        force |= 1u << t;
+        if (range_in64(c.ray, c.bp, hi, a.data_lo + (hi - a.data), c.sy, c.sx, cur[0], cur[1], cur[2], eb, xb, ns, s,
+                       tf.bound64[t][0], tf.bound64[t][1]))
+            force_in |= 1u << t;
+    }
+}
 
 // The sample position inside the cell, kept in [0, 1] (CLAMP: the walk's
 // cells contain the ray, so only float32 rounding can step outside) or
@@ -725,7 +854,7 @@ YTGB_HD float cell_coord(float x) {
     return CLAMP ? fminf(fmaxf(x, 0.0f), 1.0f) : x;
 }
 
-template <int MODE, int CTF, bool CLAMP = true, bool TG = false>
+template <int MODE, int VAR, bool CLAMP = true, bool TG = false>
 YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi, const CellCtx &c, const int cur[3],
                          const float P[3], float dtf, long long enter_bits, long long exit_bits, RayState &st) {
     st.visits++;
@@ -768,7 +897,9 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
             light_gradient(c.base + off, lo, c.sy, c.sx, fx, fy, fz, g);
             const float dot = ffma(a.light_dir[2], g[2], ffma(a.light_dir[1], g[1], fmul(a.light_dir[0], g[0])));
             float trgba[6];
-            tf_eval(a.tf, s_tab, dvs, trgba);
+            unsigned force = 0u, force_in = 0u;
+            if (VAR & V_REF) range_decisions(a, c, dvs, off, cur, enter_bits, exit_bits, ns, s, force, force_in);
+            tf_eval(a.tf, s_tab, dvs, trgba, force, force_in);
             if (a.tf.grey_opacity == 1) {
                 const float d = fmul(dts, fadd(fadd(trgba[0], trgba[1]), trgba[2]));
                 YTGB_UNROLL
@@ -815,12 +946,18 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
         const float fx = cell_coord<CLAMP>(ffma(f, c.vel[0], P[0]));
         const float fy = cell_coord<CLAMP>(ffma(f, c.vel[1], P[1]));
         const float fz = cell_coord<CLAMP>(ffma(f, c.vel[2], P[2]));
-        if (MODE == MODE_VR && CTF) {
+        if (MODE == MODE_VR && (VAR & V_CTF)) {
             const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
             const ytgb_tf &tf = a.tf;
+            bool in = !(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val);
+            if ((VAR & V_REF) && c.tol >= 0.0f && range_ambiguous(val, c.tol, tf.lo_excl[0], tf.hi_excl[0])) {
+                // decide as yt does, from the float64 value (rare)
+                in = range_in64(c.ray, c.bp, c.base + off, a.data_lo + (c.base - a.data) + off, c.sy, c.sx, cur[0],
+                                cur[1], cur[2], enter_bits, exit_bits, ns, s, tf.bound64[0][0], tf.bound64[0][1]);
+            }
             // outside the table's range: zero emission and absorption leave x
             // unchanged
-            if (!(val >= tf.hi_excl[0] || val <= tf.lo_excl[0]) && val != 0.0f && finitef(val)) {
+            if (in) {
                 float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
                 q = fminf(fmaxf(q, 0.0f), (float)(tf.nbins[0] - 2));
                 const int bin = (int)q;
@@ -867,7 +1004,10 @@ YTGB_HD void sample_cell(const ytgb_render_args &a, const float4 *s_tab, int bi,
                 if (fi < c.nf) dvs[fi] = trilinear(c.base + fi * c.fstride + off, c.sy, c.sx, fx, fy, fz);
             if (MODE == MODE_VR) {
                 float trgba[6];
-                tf_eval(a.tf, s_tab, dvs, trgba);
+                unsigned force = 0u, force_in = 0u;
+                if (VAR & V_REF)
+                    range_decisions(a, c, dvs, off, cur, enter_bits, exit_bits, ns, s, force, force_in);
+                tf_eval(a.tf, s_tab, dvs, trgba, force, force_in);
                 if (a.tf.grey_opacity == 1) {
                     const float da = fmul(dts, trgba[3]);
                     YTGB_UNROLL
@@ -940,7 +1080,7 @@ YTGB_HD void add_sel(float &h, float &l, float inc) {
 // cases (tmax leaving its binade, a step count past the bound) branch.  Every entry index inside the brick stays
 // inside until the walk leaves it (an index changes only by a step on its
 // own axis, after which the exit test runs).
-template <int MODE, int CTF, bool COMP, bool TG>
+template <int MODE, int VAR, bool COMP, bool TG>
 YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, const ytgb_brick *bp,
                         const CellCtx &c, const Walk &w, long long kmax, int step_limit, RayState &st) {
     AxisStep A0, A1, A2;
@@ -986,10 +1126,15 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
         const float fy = cell_coord<true>(ffma(f, v1, P1));
         const float fz = cell_coord<true>(ffma(f, v2, P2));
         const int off = c0 * c.sx + c1 * c.sy + c2;
-        if (MODE == MODE_VR && CTF) {
+        if (MODE == MODE_VR && (VAR & V_CTF)) {
             const float val = trilinear(c.base + off, c.sy, c.sx, fx, fy, fz);
             // (NaN and infinities fail the strict bound tests, so they need no separate test)
-            const bool in = val < tf.hi_excl[0] && val > tf.lo_excl[0] && val != 0.0f;
+            bool in = val < tf.hi_excl[0] && val > tf.lo_excl[0] && val != 0.0f;
+            if ((VAR & V_REF) && range_ambiguous(val, c.tol, tf.lo_excl[0], tf.hi_excl[0])) {
+                // decide as yt does, from the float64 value (rare)
+                in = range_in64(&r, bp, c.base + off, a.data_lo + (c.base - a.data) + off, c.sy, c.sx, c0, c1, c2, eb,
+                                xb, 1, 0, tf.bound64[0][0], tf.bound64[0][1]);
+            }
             float q = fmul(fsub(val, tf.b0[0]), tf.idbin[0]);
             q = fminf(fmaxf(q, 0.0f), nbm2);  // a NaN q gives bin 0 (the sample is then out of range)
             const int bin = (int)q;
@@ -1096,7 +1241,7 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
 // s_tab: the transfer-function tables -- as staged in shared memory (TG
 // false) or as packed in global memory (TG true, see ctf_bin); bi: the brick
 // index.
-template <int MODE, int CTF, bool TG = false>
+template <int MODE, int VAR, bool TG = false>
 YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, int bi, RayState &st) {
     const ytgb_brick *bp = a.bricks + bi;
     BrickF bf;
@@ -1126,15 +1271,23 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     c.sy = bf.dims[2] + 1;
     c.sx = (bf.dims[1] + 1) * (bf.dims[2] + 1);
     const int step_limit = bf.dims[0] + bf.dims[1] + bf.dims[2] + 3;
+    // samples near a transfer-function bound are decided in float64 where the
+    // arena carries its float32 rounding errors
+    // (the launch takes the V_REF variant only with data_lo and range_eps > 0,
+    // and for a ColorTransferFunction only when its table is not the
+    // exclude-everything form of out-of-range bounds)
+    c.tol = (VAR & V_REF) ? range_tol(a.range_eps, step_limit) : -1.0f;
+    c.ray = &r;
+    c.bp = bp;
     int hitc = 0;
     const long long b0 = dbits(w.tmax[0]), b1 = dbits(w.tmax[1]), b2 = dbits(w.tmax[2]);
     const long long INF = 0x7ff0000000000000LL;
     const bool int_path = b0 > 0 && b1 > 0 && b2 > 0 && b0 < INF && b1 < INF && b2 < INF && kmax > 0;
-    if (MODE != MODE_TRACE && MODE != MODE_LIGHT && (MODE != MODE_VR || CTF) && int_path && a.n_samples == 1 &&
+    if (MODE != MODE_TRACE && MODE != MODE_LIGHT && (MODE != MODE_VR || (VAR & V_CTF)) && int_path && a.n_samples == 1 &&
         (MODE != MODE_VR || c.moff < 0 || !a.masks) && (unsigned)w.cur[0] < (unsigned)c.dims[0] &&
         (unsigned)w.cur[1] < (unsigned)c.dims[1] && (unsigned)w.cur[2] < (unsigned)c.dims[2]) {
-        if (st.comp) cells_fast<MODE, CTF, true, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
-        else cells_fast<MODE, CTF, false, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        if (st.comp) cells_fast<MODE, VAR, true, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
+        else cells_fast<MODE, VAR, false, TG>(a, s_tab, r, bp, c, w, kmax, step_limit, st);
         return;
     }
     // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
@@ -1162,7 +1315,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
             const long long tmb = i == 0 ? A0.bits : (i == 1 ? A1.bits : A2.bits);
             const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
             const float dtf = MODE == MODE_TRACE ? 0.0f : diff_to_float(xb, eb);
-            sample_cell<MODE, CTF, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, eb, xb, st);
+            sample_cell<MODE, VAR, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, eb, xb, st);
             // advance (grid_traversal.pyx:134-138)
             const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
             advance_position(w.P, c.vel, dtf, i, si);
@@ -1203,7 +1356,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
         const long long Ki = i == 0 ? K0 : (i == 1 ? K1 : K2);
         const double exit_t = Ki < kmax ? tm : max_t;
         const float dtf = MODE == MODE_TRACE ? 0.0f : (float)dsub(exit_t, enter_t);
-        sample_cell<MODE, CTF, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
+        sample_cell<MODE, VAR, true, TG>(a, s_tab, bi, c, w.cur, w.P, dtf, dbits(enter_t), dbits(exit_t), st);
         const int si = i == 0 ? r.step[0] : (i == 1 ? r.step[1] : r.step[2]);
         advance_position(w.P, c.vel, dtf, i, si);
         const double td = i == 0 ? tdelta[0] : (i == 1 ? tdelta[1] : tdelta[2]);

@@ -117,7 +117,7 @@ __device__ __forceinline__ void stage_tf(const ytgb_render_args &a, float4 *s_ta
 //   bx, by: the block tile (TX x TY pixels); w: which 32 of its 128 pixels;
 //   tab: the transfer-function tables (shared: TG false; global: TG true);
 //   slot: this thread's ray slot in sm.ray, wl: its warp's list in sm.sel.
-template <int MODE, int CTF, int TS, bool TG>
+template <int MODE, int VAR, int TS, bool TG>
 __device__ __forceinline__ void warp_tile(const ytgb_render_args &a, int bx, int by, int w, const float4 *tab,
                                           TileSmem &sm, int slot, int wl, unsigned long long *hashes,
                                           long long *counts) {
@@ -163,7 +163,7 @@ __device__ __forceinline__ void warp_tile(const ytgb_render_args &a, int bx, int
                 const int kk = sel[j];
                 const int4 rc = __ldg(rects + kk);
                 if (vi < rc.x || vi >= rc.y || vj < rc.z || vj >= rc.w) continue;
-                walk_brick<MODE, CTF, TG>(a, tab, r, __ldg(a.order + kk), st);
+                walk_brick<MODE, VAR, TG>(a, tab, r, __ldg(a.order + kk), st);
             }
             __syncwarp();  // the list is rewritten by the next passes
             nsel = 0;
@@ -196,17 +196,17 @@ __device__ __forceinline__ void warp_tile(const ytgb_render_args &a, int bx, int
 }
 
 // One view, one tile per block (four warps of 32 pixels).
-template <int MODE, int CTF, int TS>
+template <int MODE, int VAR, int TS>
 __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
                                                        long long *counts) {
     extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;
     if (MODE == MODE_VR || MODE == MODE_LIGHT) {
-        stage_tf<CTF>(a, s_tab);
+        stage_tf<VAR & V_CTF>(a, s_tab);
         __syncthreads();
     }
     const int w = threadIdx.x >> 5;
-    warp_tile<MODE, CTF, TS, false>(a, blockIdx.y, blockIdx.x, w, s_tab, sm, threadIdx.x, w, hashes, counts);
+    warp_tile<MODE, VAR, TS, false>(a, blockIdx.y, blockIdx.x, w, s_tab, sm, threadIdx.x, w, hashes, counts);
 }
 
 // Many views in one persistent launch: every warp pulls work items -- one
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_re
 // use different tables and read them from global memory (cached).  Every
 // loop iteration takes a new item: a warp runs at most as many iterations as
 // there are items (no spin, and no barrier after the staging).
-template <int MODE, int CTF, int TS, bool STAGED>
+template <int MODE, int VAR, int TS, bool STAGED>
 __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
                                                       int total_tiles, int *queue) {
     extern __shared__ float4 s_tab[];
@@ -231,12 +231,12 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_bat
         unsigned dyn = 0;
         asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
         const ytgb_render_args &a0 = entries[0].args;
-        const size_t need = (size_t)(CTF ? 3 : a0.tf.n_fits) * a0.tf.nbins_max * sizeof(float4);
+        const size_t need = (size_t)((VAR & V_CTF) ? 3 : a0.tf.n_fits) * a0.tf.nbins_max * sizeof(float4);
         if (need > dyn) {
             if (threadIdx.x == 0) set_error(a0.error, YTGB_DEVERR_BAD_TF);
             return;
         }
-        stage_tf<CTF>(a0, s_tab);
+        stage_tf<VAR & V_CTF>(a0, s_tab);
         __syncthreads();
     }
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_bat
         const int t = tile - __ldg(&e.tile_begin);
         const int ty = __ldg(&e.tiles_y);
         const float4 *tab = STAGED ? s_tab : reinterpret_cast<const float4 *>(e.args.tf_tables);
-        warp_tile<MODE, CTF, TS, !STAGED>(e.args, t / ty, t % ty, item % NWARP, tab, sm, threadIdx.x, wl, nullptr,
+        warp_tile<MODE, VAR, TS, !STAGED>(e.args, t / ty, t % ty, item % NWARP, tab, sm, threadIdx.x, wl, nullptr,
                                          nullptr);
     }
 }
@@ -294,6 +294,10 @@ int check_args(const ytgb_render_args *a, bool trace) {
     }
     if (a->n_samples < 1) {
         ytgb_set_error("ytgb_render: n_samples must be >= 1");
+        return YTGB_ERR_INVALID;
+    }
+    if (!(a->range_eps >= 0.0f) || !(a->range_eps <= 3.0e38f)) {
+        ytgb_set_error("ytgb_render: range_eps must be finite and >= 0");
         return YTGB_ERR_INVALID;
     }
     // the kernels load these with vector / 8-byte accesses
@@ -378,7 +382,7 @@ int launch_status(const char *what) {
     return YTGB_OK;
 }
 
-template <int MODE, int CTF, int TS>
+template <int MODE, int VAR, int TS>
 int launch(const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long long *h, long long *c) {
     constexpr int TX = TileShape<TS>::X, TY = TileShape<TS>::Y;
     dim3 grid((a->view.ny + TY - 1) / TY, (a->view.nx + TX - 1) / TX);
@@ -386,29 +390,39 @@ int launch(const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long
         ytgb_set_error("ytgb_render: image too tall");
         return YTGB_ERR_INVALID;
     }
-    if (int st = set_smem(render_kernel<MODE, CTF, TS>, smem)) return st;
-    render_kernel<MODE, CTF, TS><<<grid, BLOCK, smem, s>>>(*a, h, c);
+    if (int st = set_smem(render_kernel<MODE, VAR, TS>, smem)) return st;
+    render_kernel<MODE, VAR, TS><<<grid, BLOCK, smem, s>>>(*a, h, c);
     return launch_status("render launch");
 }
 
-template <int MODE, int CTF>
+template <int MODE, int VAR>
 int launch_ts(int ts, const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long long *h, long long *c) {
     switch (ts) {
-    case 1: return launch<MODE, CTF, 1>(a, smem, s, h, c);
-    case 2: return launch<MODE, CTF, 2>(a, smem, s, h, c);
-    default: return launch<MODE, CTF, 0>(a, smem, s, h, c);
+    case 1: return launch<MODE, VAR, 1>(a, smem, s, h, c);
+    case 2: return launch<MODE, VAR, 2>(a, smem, s, h, c);
+    default: return launch<MODE, VAR, 0>(a, smem, s, h, c);
     }
 }
 
 int tile_shape_of(uint32_t flags) { return (int)((flags >> YTGB_FLAG_TILE_SHIFT) & 0xfu); }
 
-template <int MODE, int CTF, int TS>
+template <int MODE>
+int launch_var(int var, int ts, const ytgb_render_args *a, size_t smem, cudaStream_t s) {
+    switch (var) {
+    case V_CTF: return launch_ts<MODE, V_CTF>(ts, a, smem, s, nullptr, nullptr);
+    case V_REF: return launch_ts<MODE, V_REF>(ts, a, smem, s, nullptr, nullptr);
+    case V_CTF | V_REF: return launch_ts<MODE, V_CTF | V_REF>(ts, a, smem, s, nullptr, nullptr);
+    default: return launch_ts<MODE, 0>(ts, a, smem, s, nullptr, nullptr);
+    }
+}
+
+template <int MODE, int VAR, int TS>
 int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem,
                    cudaStream_t s) {
     // smem > 0: every entry shares the transfer function (ytgb_batch_plan),
     // staged in shared memory; 0: tables read from global memory
     const bool staged = smem > 0 && (MODE == MODE_VR || MODE == MODE_LIGHT);
-    auto kernel = staged ? batch_kernel<MODE, CTF, TS, true> : batch_kernel<MODE, CTF, TS, false>;
+    auto kernel = staged ? batch_kernel<MODE, VAR, TS, true> : batch_kernel<MODE, VAR, TS, false>;
     if (!staged) smem = 0;
     if (int st = set_smem(kernel, smem)) return st;
     if (blocks <= 0) {
@@ -424,13 +438,13 @@ int batch_launch_t(const ytgb_batch_entry *d, int n, int total, int *queue, int 
     return launch_status("batch launch");
 }
 
-template <int MODE, int CTF>
+template <int MODE, int VAR>
 int batch_launch_ts(int ts, const ytgb_batch_entry *d, int n, int total, int *queue, int blocks, size_t smem,
                     cudaStream_t s) {
     switch (ts) {
-    case 1: return batch_launch_t<MODE, CTF, 1>(d, n, total, queue, blocks, smem, s);
-    case 2: return batch_launch_t<MODE, CTF, 2>(d, n, total, queue, blocks, smem, s);
-    default: return batch_launch_t<MODE, CTF, 0>(d, n, total, queue, blocks, smem, s);
+    case 1: return batch_launch_t<MODE, VAR, 1>(d, n, total, queue, blocks, smem, s);
+    case 2: return batch_launch_t<MODE, VAR, 2>(d, n, total, queue, blocks, smem, s);
+    default: return batch_launch_t<MODE, VAR, 0>(d, n, total, queue, blocks, smem, s);
     }
 }
 
@@ -445,16 +459,17 @@ extern "C" int ytgb_render(const ytgb_render_args *a, void *stream) {
         ytgb_set_error("ytgb_render: unknown tile shape");
         return YTGB_ERR_INVALID;
     }
+    const int var = render_variant(*a);
     if (a->kind == YTGB_LIGHT_SOURCE) {
         size_t smem = 0;
         if ((st = tf_check(a->tf, &smem, false))) return st;
-        return launch_ts<MODE_LIGHT, 0>(ts, a, smem, s, nullptr, nullptr);
+        return (var & V_REF) ? launch_ts<MODE_LIGHT, V_REF>(ts, a, smem, s, nullptr, nullptr)
+                             : launch_ts<MODE_LIGHT, 0>(ts, a, smem, s, nullptr, nullptr);
     }
     if (a->kind == YTGB_VOLUME_RENDER) {
         size_t smem = 0;
         if ((st = tf_check(a->tf, &smem, a->tf.ctf_fast != 0))) return st;
-        return a->tf.ctf_fast ? launch_ts<MODE_VR, 1>(ts, a, smem, s, nullptr, nullptr)
-                              : launch_ts<MODE_VR, 0>(ts, a, smem, s, nullptr, nullptr);
+        return launch_var<MODE_VR>(var, ts, a, smem, s);
     }
     switch (a->kind) {
     case YTGB_PROJECTION: return launch_ts<MODE_PROJ, 0>(ts, a, 0, s, nullptr, nullptr);
@@ -482,15 +497,17 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
     const int TX = tile_shape == 1 ? 16 : (tile_shape == 2 ? 4 : 8);
     const int TY = BLOCK / TX;
     const int kind = entries[0].args.kind;
-    const int ctf = kind == YTGB_VOLUME_RENDER ? entries[0].args.tf.ctf_fast : 0;
+    const int var = render_variant(entries[0].args);
+    const int ctf = var & V_CTF;
     long long total = 0;
     size_t smem = 0;
     bool shared_tf = true;
     for (int32_t k = 0; k < n; k++) {
         ytgb_render_args &a = entries[k].args;
         if (int st = check_args(&a, false)) return st;
-        if (a.kind != kind || (kind == YTGB_VOLUME_RENDER && a.tf.ctf_fast != ctf)) {
-            ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler and table layout");
+        if (a.kind != kind || render_variant(a) != var) {
+            ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler, table layout and "
+                           "range decisions (data_lo with range_eps > 0, or neither)");
             return YTGB_ERR_INVALID;
         }
         shared_tf = shared_tf && same_tf(a, entries[0].args);
@@ -514,12 +531,38 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
     return YTGB_OK;
 }
 
-extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t ctf_fast,
+// A batch launch of one sampler kind and variant (YTGB_VARIANT_* bits, the
+// kernels' V_CTF / V_REF).
+static_assert(YTGB_VARIANT_CTF == V_CTF && YTGB_VARIANT_RANGE64 == V_REF, "variant bits");
+static int batch_dispatch(int32_t kind, int32_t variant, int32_t tile_shape, const ytgb_batch_entry *entries, int32_t n,
+                   int32_t total_tiles, int32_t *queue, int32_t blocks, size_t smem, cudaStream_t s) {
+    const bool ref = (variant & YTGB_VARIANT_RANGE64) != 0;
+    switch (kind) {
+    case YTGB_VOLUME_RENDER:
+        if (variant & YTGB_VARIANT_CTF)
+            return ref ? batch_launch_ts<MODE_VR, V_CTF | V_REF>(tile_shape, entries, n, total_tiles, queue, blocks,
+                                                                 smem, s)
+                       : batch_launch_ts<MODE_VR, V_CTF>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
+        return ref ? batch_launch_ts<MODE_VR, V_REF>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s)
+                   : batch_launch_ts<MODE_VR, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
+    case YTGB_LIGHT_SOURCE:
+        return ref ? batch_launch_ts<MODE_LIGHT, V_REF>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s)
+                   : batch_launch_ts<MODE_LIGHT, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
+    case YTGB_PROJECTION:
+        return batch_launch_ts<MODE_PROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
+    case YTGB_INTERPOLATED_PROJECTION:
+        return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
+    default:
+        return batch_launch_ts<MODE_MIP, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
+    }
+}
+
+extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, int32_t kind, int32_t variant,
                                  int32_t tile_shape, int32_t total_tiles, int32_t smem_bytes, int32_t *d_queue,
                                  int32_t blocks, void *stream) {
     if (!d_entries || n <= 0 || total_tiles <= 0 || !d_queue || tile_shape < 0 || tile_shape > 2 || kind < 0 ||
         kind > 4 || smem_bytes < 0 || smem_bytes > 200 * 1024 || ((uintptr_t)d_entries & 15) != 0 ||
-        ((uintptr_t)d_queue & 3) != 0) {
+        ((uintptr_t)d_queue & 3) != 0 || variant < 0 || variant > 3) {
         ytgb_set_error("ytgb_batch_render: bad arguments");
         return YTGB_ERR_INVALID;
     }
@@ -529,20 +572,8 @@ extern "C" int ytgb_batch_render(const ytgb_batch_entry *d_entries, int32_t n, i
         ytgb_set_error(std::string("ytgb_batch_render: ") + cudaGetErrorString(e));
         return YTGB_ERR_CUDA;
     }
-    const size_t smem = (size_t)smem_bytes;
-    switch (kind) {
-    case YTGB_VOLUME_RENDER:
-        return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s)
-                        : batch_launch_ts<MODE_VR, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s);
-    case YTGB_LIGHT_SOURCE:
-        return batch_launch_ts<MODE_LIGHT, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, smem, s);
-    case YTGB_PROJECTION:
-        return batch_launch_ts<MODE_PROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
-    case YTGB_INTERPOLATED_PROJECTION:
-        return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
-    default:
-        return batch_launch_ts<MODE_MIP, 0>(tile_shape, d_entries, n, total_tiles, d_queue, blocks, 0, s);
-    }
+    return batch_dispatch(kind, variant, tile_shape, d_entries, n, total_tiles, d_queue, blocks,
+                          (size_t)smem_bytes, s);
 }
 
 // ---- ytgb_batch_render_noalloc: the persistent batch with static scratch --
@@ -615,7 +646,7 @@ int noalloc_scratch(unsigned char **out) {
 // entry's tables into smem_bytes of shared memory and maps work items to
 // tiles by this numbering, so a mismatch would write out of bounds or
 // mis-tile an image; with the table on the host it is checked for free.
-int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32_t ctf_fast, int32_t tile_shape,
+int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32_t variant, int32_t tile_shape,
                        int32_t total_tiles, int32_t smem_bytes) {
     const int TX = tile_shape == 1 ? 16 : (tile_shape == 2 ? 4 : 8);
     const int TY = BLOCK / TX;
@@ -626,14 +657,14 @@ int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32
         const ytgb_render_args &a = h[k].args;
         shared_tf = shared_tf && same_tf(a, h[0].args);
         if (int st = check_args(&a, false)) return st;
-        if (a.kind != kind || (kind == YTGB_VOLUME_RENDER && (a.tf.ctf_fast != 0) != (ctf_fast != 0))) {
+        if (a.kind != kind || render_variant(a) != variant) {
             ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
-                           " is not of the launch's sampler kind / table layout");
+                           " is not of the launch's sampler kind / variant");
             return YTGB_ERR_INVALID;
         }
         if (kind == YTGB_VOLUME_RENDER || kind == YTGB_LIGHT_SOURCE) {
             size_t sm = 0;
-            if (int st = tf_check(a.tf, &sm, kind == YTGB_VOLUME_RENDER && ctf_fast != 0)) return st;
+            if (int st = tf_check(a.tf, &sm, kind == YTGB_VOLUME_RENDER && (variant & V_CTF) != 0)) return st;
             smem = sm > smem ? sm : smem;
         }
         const long long tx = (a.view.nx + TX - 1) / TX, ty = (a.view.ny + TY - 1) / TY;
@@ -660,7 +691,7 @@ int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32
 }  // namespace
 
 extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int32_t n, int32_t kind,
-                                         int32_t ctf_fast, int32_t tile_shape, int32_t total_tiles,
+                                         int32_t variant, int32_t tile_shape, int32_t total_tiles,
                                          int32_t smem_bytes, int32_t blocks, void *stream) {
     if (n > YTGB_NOALLOC_MAX_ENTRIES) {
         ytgb_set_error("ytgb_batch_render_noalloc: " + std::to_string(n) + " entries exceed the static scratch (" +
@@ -669,11 +700,11 @@ extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int3
         return YTGB_ERR_INVALID;
     }
     if (!h_entries || n <= 0 || total_tiles <= 0 || tile_shape < 0 || tile_shape > 2 || kind < 0 || kind > 4 ||
-        smem_bytes < 0 || smem_bytes > 200 * 1024) {
+        smem_bytes < 0 || smem_bytes > 200 * 1024 || variant < 0 || variant > 3) {
         ytgb_set_error("ytgb_batch_render_noalloc: bad arguments");
         return YTGB_ERR_INVALID;
     }
-    if (int st = noalloc_check_plan(h_entries, n, kind, ctf_fast, tile_shape, total_tiles, smem_bytes)) return st;
+    if (int st = noalloc_check_plan(h_entries, n, kind, variant, tile_shape, total_tiles, smem_bytes)) return st;
     unsigned char *base = nullptr;
     if (int st = noalloc_scratch(&base)) return st;
     int32_t *queue = reinterpret_cast<int32_t *>(base);
@@ -690,20 +721,7 @@ extern "C" int ytgb_batch_render_noalloc(const ytgb_batch_entry *h_entries, int3
         ytgb_set_error(std::string("ytgb_batch_render_noalloc: ") + cudaGetErrorString(e));
         return YTGB_ERR_CUDA;
     }
-    const size_t smem = (size_t)smem_bytes;
-    switch (kind) {
-    case YTGB_VOLUME_RENDER:
-        return ctf_fast ? batch_launch_ts<MODE_VR, 1>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s)
-                        : batch_launch_ts<MODE_VR, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
-    case YTGB_LIGHT_SOURCE:
-        return batch_launch_ts<MODE_LIGHT, 0>(tile_shape, entries, n, total_tiles, queue, blocks, smem, s);
-    case YTGB_PROJECTION:
-        return batch_launch_ts<MODE_PROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
-    case YTGB_INTERPOLATED_PROJECTION:
-        return batch_launch_ts<MODE_IPROJ, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
-    default:
-        return batch_launch_ts<MODE_MIP, 0>(tile_shape, entries, n, total_tiles, queue, blocks, 0, s);
-    }
+    return batch_dispatch(kind, variant, tile_shape, entries, n, total_tiles, queue, blocks, (size_t)smem_bytes, s);
 }
 
 extern "C" int ytgb_check_error(const int32_t *d_error, void *stream) {

@@ -88,12 +88,18 @@ class _Plain:
 
 class RenderServer:
     def __init__(self, volumes: dict, tfs: dict, device="cuda", hbm_budget=8 << 30, slots=4, max_batch=64,
-                 tile_shape=None, keep_images=False, plain=False):
+                 tile_shape=None, keep_images=False, plain=False, range64=True):
         """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name ->
         transfer function.  ``plain``: one single-view launch per request
         on one stream (``slots`` and ``max_batch`` are then 1).
         ``keep_images``: keep every finished request's image (True), none
-        (False), or those a predicate of the request selects."""
+        (False), or those a predicate of the request selects.
+        ``range64``: resident volumes also keep their values' float32
+        rounding errors (twice the device memory), so that a sample near a
+        transfer-function bound is kept or dropped as yt's float64 test
+        decides (field_interpolation_tables.pxd:72-73) -- a transfer
+        function whose bounds lie inside the data's range otherwise drops or
+        keeps a few such samples differently."""
         self.device = torch.device(device)
         self.plain = bool(plain)
         if self.plain:
@@ -104,7 +110,9 @@ class RenderServer:
         from .volume import BrickSet
 
         for name, (bricks, kd) in volumes.items():
-            self.volumes[name] = (BrickSet(bricks, device=self.device), kd)
+            bs = BrickSet(bricks, device=self.device, with_lo=range64)
+            bs.range_eps  # its one synchronising reduction, here rather than in the request loop
+            self.volumes[name] = (bs, kd)
         self.tfs = {name: (tf, pack(tf)) for name, tf in tfs.items()}
         self.budget = int(hbm_budget)
         self.in_use = 0

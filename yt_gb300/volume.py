@@ -210,10 +210,14 @@ class BrickSet:
             _lib.check(L.ytgb_gather_masks(msrc.ctypes.data, mcnt.ctypes.data, mdst.ctypes.data, mbrick.ctypes.data,
                                            mbrick.size, self.masks.data_ptr(), mlen, self.desc.data_ptr(), n,
                                            C.c_void_p(stream.cuda_stream)), "ytgb_gather_masks")
+        self._range_eps = None
+        # with_lo: the padding between fields is zeroed, so that range_eps can
+        # take the arena's largest value over the whole buffer
+        alloc = torch.zeros if with_lo else torch.empty
         if direct:
             # the device reads the caller's float64 arrays over the CPU-GPU
             # link and writes the float32 arena itself
-            buf = torch.empty((arena_len,), dtype=torch.float32, device=self.device)
+            buf = alloc((arena_len,), dtype=torch.float32, device=self.device)
             buf_lo = torch.empty((arena_len,), dtype=torch.float32, device=self.device) if with_lo else None
             stream = torch.cuda.current_stream(self.device)
             _lib.check(L.ytgb_gather_fields(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data, len(src),
@@ -231,6 +235,7 @@ class BrickSet:
             buf = _pinned((arena_len,), torch.float32, self.device)
             buf_lo = _pinned((arena_len,), torch.float32, self.device) if with_lo else None
             if with_lo:
+                buf.zero_()
                 _lib.check(L.ytgb_pack_fields_split(src.ctypes.data, fsize.ctypes.data, dst_f.ctypes.data,
                                                     len(src), buf.data_ptr(), buf_lo.data_ptr(), 0),
                            "ytgb_pack_fields_split")
@@ -242,6 +247,23 @@ class BrickSet:
         self.nbytes = int(self.data.numel() * 4)
         self.upload_bytes = int(self.data.numel() * 4 * (2 if with_lo else 1) + self.bounds.numel() * 8 +
                                 self.desc.numel() + (self.masks.numel() if self.masks is not None else 0))
+
+    @property
+    def range_eps(self) -> float:
+        """The scale of the float64 range decisions (``ytgb_render_args.
+        range_eps``): M * 2^-24, M the largest finite |value| of the arena,
+        computed from the device arena on first use (one synchronising
+        reduction) and kept; 0 without ``data_lo`` (float32 decisions)."""
+        if self.data_lo is None:
+            return 0.0
+        if self._range_eps is None:
+            m = float(torch.nan_to_num(self.data.abs(), nan=0.0, posinf=0.0).max()) if self.data.numel() else 0.0
+            self._range_eps = m * 2.0 ** -24
+        return self._range_eps
+
+    def data_changed(self):
+        """Forget range_eps after the arena was (re)written in place."""
+        self._range_eps = None
 
     def _scan_python(self, bricks, n, dims, le, re, nfields):
         """The brick scan in Python (any array types): field addresses and
@@ -315,8 +337,9 @@ class BrickSet:
         desc["mask_offset"][:] = -1
         self.desc_host = desc
         self.host = desc.ctypes.data_as(C.POINTER(_lib.Brick))
-        self.data = torch.empty(max(total, 4), dtype=torch.float32, device=self.device)
+        self.data = (torch.zeros if with_lo else torch.empty)(max(total, 4), dtype=torch.float32, device=self.device)
         self.data_lo = torch.empty_like(self.data) if with_lo else None
+        self._range_eps = None
         self.masks = None
         self.bounds = torch.from_numpy(np.ascontiguousarray(bounds)).to(self.device)
         self.desc = torch.from_numpy(desc.view(np.uint8).copy()).to(self.device)
@@ -374,7 +397,15 @@ def set_light(args, bricks, light):
         args.light_dir[i] = float(ld[i])
     for i in range(4):
         args.light_rgba[i] = float(rgba[i])
+    set_range(args, bricks)
+
+
+def set_range(args, bricks):
+    """The arena's float32 rounding errors and their scale, for the float64
+    range decisions near a transfer-function bound (volume rendering and
+    light source; none when the bricks carry no ``data_lo``)."""
     args.data_lo = _ptr(bricks.data_lo)
+    args.range_eps = bricks.range_eps
 
 
 def _ptr(t):
@@ -525,6 +556,8 @@ def render(bricks: BrickSet, view: _lib.View, order: np.ndarray, kind: int, imag
     args.zbuffer = _ptr(zbuffer)
     if kind == _lib.LIGHT_SOURCE:
         set_light(args, bricks, light)
+    elif kind == _lib.VOLUME_RENDER:
+        set_range(args, bricks)
     args.counters = _ptr(counters)
     args.error = _ptr(error)
     st = _lib.lib().ytgb_render(C.byref(args), C.c_void_p(stream.cuda_stream))
