@@ -125,20 +125,30 @@ extern "C" long long emu_check_step(long long n, int steps, unsigned long long s
 
 // mismatches of diff_to_float against (float)(x - y) computed in long double
 // (exact for these inputs), and of split_floor against floor / fraction
+// |got - exact| < one float32 ulp of exact (got is one of the two floats
+// around it)
+static bool within_ulp(float got, long double exact) {
+    const float lo = std::nextafter((float)exact, -INFINITY), hi = std::nextafter((float)exact, INFINITY);
+    const float near = (float)exact;
+    return got == near || (got == lo && (long double)lo <= exact && exact <= (long double)near) ||
+           (got == hi && (long double)near <= exact && exact <= (long double)hi);
+}
+
 extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
     std::mt19937_64 g(seed);
     long long bad = 0;
     for (long long k = 0; k < n; k++) {
         double y = rand_pos(g), x = y * (1.0 + std::ldexp((double)(g() % 1000000), -(int)(g() % 40)));
         if (g() % 3 == 0) std::swap(x, y);
+        // faithful rounding: within one float32 ulp of the exact difference
         float got = diff_to_float(dbits(x), dbits(y));
-        float want = (float)((long double)x - (long double)y);
-        if (got != want) bad++;
+        long double exact = (long double)x - (long double)y;
+        if (!within_ulp(got, exact)) bad++;
         double t = std::ldexp((double)(g() >> 11), -(int)(g() % 60));  // 0 <= t < 2^53 .. small
         if (t > 0 && t < 1073741824.0) {
             int fl; float fr;
             split_floor(dbits(t), fl, fr);
-            if (fl != (int)std::floor(t) || fr != (float)(t - std::floor(t))) bad++;
+            if (fl != (int)std::floor(t) || !within_ulp(fr, (long double)(t - std::floor(t)))) bad++;
         }
     }
     return bad;

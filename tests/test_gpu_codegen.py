@@ -4,7 +4,7 @@ Every float operation of the samplers is an explicit round-to-nearest
 intrinsic (and the float64 walk is never contracted), so how the compiler
 allocates registers, schedules or spills must not change a single bit.  This
 test compiles a second copy of the sampler kernels for 4 resident blocks per
-SM (128 registers a thread) instead of the library's 5 (96), loads it beside
+SM (128 registers a thread) instead of the library's 6 and 5 (80 and 96), loads it beside
 the library, and renders every sampler path through both: the persistent
 batch kernel and the single-view kernel of either build give bit-identical
 images, and one view matches the float64 oracle.

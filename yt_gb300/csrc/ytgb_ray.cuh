@@ -136,16 +136,21 @@ YTGB_HD float scaled_to_float(unsigned long long F, int k) {
     return ffrom(((uint32_t)(e + 127) << 23) | (uint32_t)(sig & 0x7fffffull));
 }
 
-// F * 2^k as float for F < 2^54: one rounding of F to float (the hardware
-// integer conversion, round to nearest even), then an exact scaling by a
+// F * 2^k as float for F < 2^54, faithfully rounded (one of the two floats
+// around it): F's high 22 bits (exact as a float) times 2^32 plus its low
+// 32 bits rounded to float, in one FMA -- the low part's rounding (< 2^7) is
+// under a quarter ulp of any result >= 2^32 -- then an exact scaling by a
 // power of two while the result stays in float's normal range; otherwise
-// the bit-level rounding above.  Both give the float nearest to F * 2^k.
+// the bit-level rounding above (the nearest float).  32-bit conversions
+// keep the per-cell dt off the float64 pipe, which a 64-bit conversion
+// uses (3 % of the benchmark frame).
 YTGB_HD float scaled_to_float_fast(unsigned long long F, int k) {
     if (k < -126 || k > 127 - 54) return scaled_to_float(F, k);
+    const unsigned hi = (unsigned)(F >> 32), lo = (unsigned)F;
 #ifdef __CUDA_ARCH__
-    const float f = __ull2float_rn(F);
+    const float f = ffma(__uint2float_rn(hi), 4294967296.0f, __uint2float_rn(lo));
 #else
-    const float f = (float)F;
+    const float f = ffma((float)hi, 4294967296.0f, (float)lo);
 #endif
     return fmul(f, ffrom((uint32_t)(k + 127) << 23));
 }
@@ -234,7 +239,12 @@ struct Ray {
     double dir[3];
     double iv[3];
     float fpos[3], fdir[3];
+    float ifd[3];     // 1 / fdir in float32, correctly rounded (the pre-tests)
     int step[3];
+    // tdelta = step * iv_dir * dds (grid_traversal.pyx:86) for the dds of the
+    // last brick walked (per axis): the bricks of one AMR level share their
+    // dds bit for bit, so a ray's walks within a level reuse the product
+    double td_dds[3], td[3];
 };
 
 // generate_vector_info_plane_parallel (lenses.pyx:179-192) and
@@ -282,7 +292,20 @@ YTGB_HD void make_ray(const ytgb_view &v, int vi, int vj, Ray &r) {
         r.iv[i] = r.step[i] != 0 ? ddiv(1.0, r.dir[i]) : 0.0;
         r.fpos[i] = (float)r.pos[i];
         r.fdir[i] = (float)r.dir[i];
+        r.ifd[i] = frcp(r.fdir[i]);  // = 1.0f / fdir, correctly rounded
+        r.td_dds[i] = -1.0;          // no brick has a negative dds
+        r.td[i] = 0.0;
     }
+}
+
+// tdelta of axis i for a brick with cell width dds: the ray's kept product
+// when dds is the one it was formed with, else formed (and kept) now.
+YTGB_HD double ray_tdelta(Ray &r, int i, double dds) {
+    if (dbits(r.td_dds[i]) != dbits(dds)) {
+        r.td_dds[i] = dds;
+        r.td[i] = dmul(dmul((double)r.step[i], r.iv[i]), dds);
+    }
+    return r.td[i];
 }
 
 // Brick data for the float32 pre-tests (loaded for every candidate brick).
@@ -1086,7 +1109,7 @@ YTGB_HD void add_sel(float &h, float &l, float inc) {
 // off but still issued (one field: the projection 24 % and the MIP 27 %
 // faster with NCH = 1).  GREY: grey_opacity fixed (0 or 1) or read (-1).
 template <int MODE, int VAR, bool COMP, bool TG, int NCH = 0, int GREY = -1>
-YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, const ytgb_brick *bp,
+YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, Ray &r, const ytgb_brick *bp,
                         const CellCtx &c, const Walk &w, long long kmax, int step_limit, RayState &st) {
     AxisStep A0, A1, A2;
     A0.bits = dbits(w.tmax[0]);
@@ -1094,9 +1117,9 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
     A2.bits = dbits(w.tmax[2]);
     {
         // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
-        const double t0 = dmul(dmul((double)r.step[0], r.iv[0]), ldg(&bp->dds[0]));
-        const double t1 = dmul(dmul((double)r.step[1], r.iv[1]), ldg(&bp->dds[1]));
-        const double t2 = dmul(dmul((double)r.step[2], r.iv[2]), ldg(&bp->dds[2]));
+        const double t0 = ray_tdelta(r, 0, ldg(&bp->dds[0]));
+        const double t1 = ray_tdelta(r, 1, ldg(&bp->dds[1]));
+        const double t2 = ray_tdelta(r, 2, ldg(&bp->dds[2]));
         step_prepare(A0, t0);
         step_prepare(A1, t1);
         step_prepare(A2, t2);
@@ -1211,11 +1234,9 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
         A2.bits = s2 ? nb : A2.bits;
         if (md == 3 || (int)(nb >> 52) != ex) {
             // tmax leaves its binade (or has no integer step): the float64 add
-            // (selects rather than r.iv[i]: a runtime index would put the ray in local memory)
+            // (the ray is in shared memory: a runtime index costs no local memory)
             const int i = s0 ? 0 : (s1 ? 1 : 2);
-            const int sti = s0 ? r.step[0] : (s1 ? r.step[1] : r.step[2]);
-            const double ivi = s0 ? r.iv[0] : (s1 ? r.iv[1] : r.iv[2]);
-            const double td = dmul(dmul((double)sti, ivi), ldg(&bp->dds[i]));
+            const double td = r.td[i];  // (kept by the prologue for this brick)
             const long long sb = dbits(dadd(dfrom(tmb), td));
             if (s0) {
                 A0.bits = sb;
@@ -1247,16 +1268,14 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, const Ra
 // false) or as packed in global memory (TG true, see ctf_bin); bi: the brick
 // index.
 template <int MODE, int VAR, bool TG = false>
-YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ray &r, int bi, RayState &st) {
+YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, Ray &r, int bi, RayState &st) {
     const ytgb_brick *bp = a.bricks + bi;
     BrickF bf;
     load_brick_f(bp, bf);
-    // 1 / v_dir in float32 for the float32 pre-tests (a product with it is
-    // within two float32 roundings of the quotient; their margins are 1e-5
+    // r.ifd: 1 / v_dir in float32 for the float32 pre-tests (a product with it
+    // is within two float32 roundings of the quotient; their margins are 1e-5
     // and 1e-4 of the operands' scale)
-    float ifd[3];
-    YTGB_UNROLL
-    for (int i = 0; i < 3; i++) ifd[i] = frcp(r.fdir[i]);  // = 1.0f / fdir, correctly rounded
+    const float ifd[3] = {r.ifd[0], r.ifd[1], r.ifd[2]};
     if (surely_misses(bf, r, ifd, st.max_tf)) return;
     const double max_t = st.max_t;
     const long long kmax = dkey(st.max_t);
@@ -1306,7 +1325,7 @@ YTGB_HD void walk_brick(const ytgb_render_args &a, const float4 *s_tab, const Ra
     // tdelta = step * iv_dir * dds (grid_traversal.pyx:86)
     double tdelta[3];
     YTGB_UNROLL
-    for (int i = 0; i < 3; i++) tdelta[i] = dmul(dmul((double)r.step[i], r.iv[i]), ldg(&bp->dds[i]));
+    for (int i = 0; i < 3; i++) tdelta[i] = ray_tdelta(r, i, ldg(&bp->dds[i]));
     if (int_path) {
         // ---- integer cell loop (positive walk values: key == bits) -----------
         AxisStep A0, A1, A2;

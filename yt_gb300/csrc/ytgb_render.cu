@@ -64,17 +64,20 @@ template <> struct TileShape<1> { static constexpr int X = 16, Y = 8; };
 template <> struct TileShape<2> { static constexpr int X = 4, Y = 32; };
 constexpr int BLOCK = 128;
 constexpr int NWARP = BLOCK / 32;
-// Resident blocks per SM the kernels are compiled for (at most 96 registers
-// a thread).  The per-ray walk is latency-bound (dependent integer and
-// float64 steps), so warps per SM count for more than registers: with the
-// rays held in shared memory the 96-register build does not spill, and on
-// the 1024^2 AMR frame it runs 1.30 ms against 1.28 ms at 6 blocks (80
-// registers, spilling) and 1.42 ms at 7; the 64-view batch prefers 5 (37.0
-// against 40.0 and 39.0 ms).  Images are identical at every setting.
-#ifndef YTGB_MIN_BLOCKS
-#define YTGB_MIN_BLOCKS 5
+// Resident blocks per SM the kernels are compiled for.  The per-ray walk is
+// latency-bound (dependent integer and float64 steps), so warps per SM
+// count for more than registers.  The single-view kernel takes 6 (80
+// registers, a few spills in the per-walk state): on the 1024^2 AMR frame
+// 1.199 ms against 1.234 ms at 5 (96 registers, no spills), and the
+// projections 3-6 % faster.  The persistent batch kernel, whose loop keeps
+// more state, takes 5: the 64-view batch runs 32.7 ms against 33.2 ms at
+// 6.  Images are identical at every setting.  YTGB_MIN_BLOCKS sets both
+// (a second build at another budget, for the bit-identity test).
+#ifdef YTGB_MIN_BLOCKS
+constexpr int MIN_BLOCKS = YTGB_MIN_BLOCKS, BATCH_MIN_BLOCKS = YTGB_MIN_BLOCKS;
+#else
+constexpr int MIN_BLOCKS = 6, BATCH_MIN_BLOCKS = 5;
 #endif
-constexpr int MIN_BLOCKS = YTGB_MIN_BLOCKS;
 
 // Selected bricks a warp holds before walking them (flushed in order when
 // nearly full).
@@ -220,7 +223,7 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_re
 // loop iteration takes a new item: a warp runs at most as many iterations as
 // there are items (no spin, and no barrier after the staging).
 template <int MODE, int VAR, int TS, bool STAGED>
-__global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
+__global__ void __launch_bounds__(BLOCK, BATCH_MIN_BLOCKS) batch_kernel(const ytgb_batch_entry *entries, int n_entries,
                                                       int total_tiles, int *queue) {
     extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;

@@ -11,7 +11,12 @@ over time.  The loop:
   a lone request takes the single-view kernel) as soon as one of ``slots``
   CUDA streams is free -- so requests that arrive while earlier batches are
   on the GPU start on another stream at once and their work overlaps on the
-  device (continuous batching, not a queue in front of one stream);
+  device (continuous batching, not a queue in front of one stream).  Each
+  launch takes a stream one priority level below every batch still in
+  flight: the block scheduler gives SMs to the earliest batch's blocks
+  first and lets later batches fill what it leaves, so a request is not
+  slowed by requests that arrived after it (first come, first served, with
+  backfill) -- the plain loop's order without its idle SMs;
 * **retires** a batch when its completion event fires, frees its images'
   budget and records each request's latency (completion - arrival);
 * **drops** requests cancelled before their launch (``Request.cancelled``),
@@ -67,6 +72,15 @@ class Request:
         return self.done - self.arrival
 
 
+PRIORITY_LEVELS = 4  # stream priorities the served launches use (0 .. -3)
+
+
+def launch_level(levels_in_flight) -> int:
+    """The priority level of a new launch (0 the highest): one below every
+    batch still in flight, the lowest level once that is reached."""
+    return min(PRIORITY_LEVELS - 1, max((k + 1 for k in levels_in_flight), default=0))
+
+
 @dataclass
 class _InFlight:
     requests: list
@@ -76,6 +90,7 @@ class _InFlight:
     counters: torch.Tensor
     error: torch.Tensor
     keep: list = field(default_factory=list)   # device inputs the launch reads
+    level: int = 0                             # its stream's priority level (0 the highest)
 
 
 class _Plain:
@@ -116,7 +131,12 @@ class RenderServer:
         self.tfs = {name: (tf, pack(tf)) for name, tf in tfs.items()}
         self.budget = int(hbm_budget)
         self.in_use = 0
-        self.slots = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.n_slots = slots
+        # slots streams per priority level, level 0 the highest (CUDA: lower
+        # numbers are higher priorities; torch keeps PRIORITY_LEVELS pools)
+        self.levels = [[torch.cuda.Stream(self.device, priority=-(PRIORITY_LEVELS - 1 - k)) for _ in range(slots)]
+                       for k in range(PRIORITY_LEVELS)]
+        self.slots = self.levels[0]
         self.max_batch = max_batch
         self.tile_shape = tile_shape
         self.keep_images = keep_images
@@ -187,7 +207,6 @@ class RenderServer:
         pending = deque(sorted(requests, key=lambda q: q.arrival))
         admitted = deque()
         inflight: list[_InFlight] = []
-        free = list(self.slots)
         t0 = time.perf_counter()
         done = []
         while pending or admitted or inflight:
@@ -216,7 +235,6 @@ class RenderServer:
                     self.in_use -= f.bytes
                     self.samples += int(f.counters[0].item())
                     _lib.check(_lib.lib().ytgb_check_error(f.error.data_ptr(), f.stream.cuda_stream), "serve")
-                    free.append(f.stream)
                     inflight.remove(f)
                     done += f.requests
             if self.on_tick is not None:
@@ -232,10 +250,17 @@ class RenderServer:
                 q.admitted = now
                 self.in_use += q.image_bytes
                 admitted.append(q)
-            # launch everything admitted on a free slot
+            # launch everything admitted on a free slot, one priority level
+            # below the batches in flight
+            free = len(inflight) < self.n_slots
             if admitted and free:
                 reqs = [admitted.popleft() for _ in range(min(self.max_batch, len(admitted)))]
-                inflight.append(self._launch(reqs, free.pop(), now))
+                level = launch_level(f.level for f in inflight)
+                busy = {f.stream for f in inflight}
+                stream = next(st for st in self.levels[level] if st not in busy)
+                f = self._launch(reqs, stream, now)
+                f.level = level
+                inflight.append(f)
                 continue
             if not admitted and (not pending or pending[0].arrival > now):
                 # nothing to launch: wait briefly for arrivals or completions
