@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--served-requests", type=int, default=100, help="requests per rate in the default line")
     ap.add_argument("--max-batch", type=int, default=64, help="requests per served batch (--workload serve)")
     ap.add_argument("--slots", type=int, default=4, help="streams of the render server (--workload serve)")
+    ap.add_argument("--batch-pixels", type=int, default=512 * 512,
+                    help="requests under this many pixels share a batch launch (--workload serve)")
     return ap.parse_args()
 
 
@@ -778,7 +780,7 @@ def serve_requests(vols, n, rate, seed):
     return out
 
 
-def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slots=4):
+def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slots=4, batch_pixels=512 * 512):
     """Served rendering against plain: at each rate the same Poisson stream
     goes through the render server (HBM-budget admission, continuous
     batching on four streams) and through the plain form (one single-view
@@ -790,7 +792,8 @@ def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slo
     from yt_gb300.serve import RenderServer, latency_summary
 
     vols, tfs, t_build = serve_volumes(dev, amr)
-    srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=slots, max_batch=max_batch)
+    srv = RenderServer(vols, tfs, device=dev, hbm_budget=16 << 30, slots=slots, max_batch=max_batch,
+                       batch_pixels=batch_pixels)
     plain_srv = RenderServer({}, {}, device=dev, hbm_budget=16 << 30, plain=True)
     plain_srv.volumes, plain_srv.tfs = srv.volumes, srv.tfs
     # warm-up: compile paths, stage tables
@@ -847,6 +850,7 @@ def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slo
                       "vs": "float64 oracle", "sample": "every 100th served request"
                       + (f", {audit} of them spread evenly" if audit is not None else "")},
             "requests_per_rate": n_requests, "slots": slots, "max_batch": max_batch, "hbm_budget_gib": 16,
+            "batch_pixels": batch_pixels,
             "plain": "the same requests, one render_kernel launch each, one stream, in arrival order",
             "clocks": clocks.summary(), "build_seconds": t_build}
 
@@ -856,7 +860,8 @@ def run_serve(args):
 
     dev = torch.device("cuda", 0)
     rates = [float(x) for x in args.rates.split(",")]
-    rec = serve_record(dev, args.n_requests, rates, audit=args.audit, max_batch=args.max_batch, slots=args.slots)
+    rec = serve_record(dev, args.n_requests, rates, audit=args.audit, max_batch=args.max_batch, slots=args.slots,
+                       batch_pixels=args.batch_pixels)
     line = {"metric": "Gsamples/s & p50/p99 latency", "workload": "serve", "value": rec["value"],
             "unit": "Gsamples/s", "n_gpus": 1, "higher_is_better": True, "served": rec}
     print(json.dumps(line), flush=True)

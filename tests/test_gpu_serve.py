@@ -39,11 +39,16 @@ def requests(n, seed=0, rate=None):
     return out
 
 
-def test_alone_equals_mixed(cuda):
-    srv, w1, w2 = make_server(cuda, keep_images=True, slots=3, max_batch=8)
+@pytest.mark.parametrize("batch_pixels", [0, 40 * 40, 1 << 30])
+def test_alone_equals_mixed(cuda, batch_pixels):
+    """Every request's image is the same alone and in the mix, whether the
+    group renders through the batch kernel (all small), the single-view
+    kernel (all large) or both."""
+    srv, w1, w2 = make_server(cuda, keep_images=True, slots=3, max_batch=8, batch_pixels=batch_pixels)
     reqs = requests(24)
     done = srv.run(reqs, realtime=False)
     assert len(done) == 24 and all(q.done >= q.arrival for q in done)
+    assert all(q.done >= q.launched for q in done)
     for q in done:
         alone = srv.renderer(q.volume, q.tf).render(q.camera)
         assert torch.equal(alone.view(torch.int64), q.image.view(torch.int64)), q.rid

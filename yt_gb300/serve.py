@@ -6,10 +6,12 @@ over time.  The loop:
 
 * **admits** arrived requests while their output images fit the HBM budget
   (a request waits in the arrival queue otherwise);
-* **batches** every admitted, not yet launched request into one
-  :class:`~yt_gb300.batch.Batch` (one persistent launch per sampler class;
-  a lone request takes the single-view kernel) as soon as one of ``slots``
-  CUDA streams is free -- so requests that arrive while earlier batches are
+* **batches** every admitted, not yet launched request into one group as
+  soon as one of ``slots`` CUDA streams is free: the small requests of the
+  group go into one :class:`~yt_gb300.batch.Batch` (one persistent launch
+  per sampler class), the large ones -- which fill the GPU by themselves --
+  and a lone small one take the single-view kernel one after another on
+  the same stream, each request finishing with its own launch -- so requests that arrive while earlier batches are
   on the GPU start on another stream at once and their work overlaps on the
   device (continuous batching, not a queue in front of one stream).  Each
   launch takes a stream one priority level below every batch still in
@@ -63,9 +65,13 @@ class Request:
     batch_size: int = 0           # requests in the launch that rendered it
 
     @property
-    def image_bytes(self) -> int:
+    def pixels(self) -> int:
         nx, ny = self.camera.resolution
-        return nx * ny * 4 * 8
+        return nx * ny
+
+    @property
+    def image_bytes(self) -> int:
+        return self.pixels * 4 * 8
 
     @property
     def latency(self) -> float:
@@ -83,13 +89,12 @@ def launch_level(levels_in_flight) -> int:
 
 @dataclass
 class _InFlight:
-    requests: list
-    event: torch.cuda.Event
+    parts: list                                # [(requests, completion event)] in stream order
     stream: torch.cuda.Stream
     bytes: int
-    counters: torch.Tensor
-    error: torch.Tensor
-    keep: list = field(default_factory=list)   # device inputs the launch reads
+    counters: list                             # counter tensors of its launches
+    errors: list                               # error words of its launches
+    keep: list = field(default_factory=list)   # device inputs the launches read
     level: int = 0                             # its stream's priority level (0 the highest)
 
 
@@ -103,7 +108,7 @@ class _Plain:
 
 class RenderServer:
     def __init__(self, volumes: dict, tfs: dict, device="cuda", hbm_budget=8 << 30, slots=4, max_batch=64,
-                 tile_shape=None, keep_images=False, plain=False, range64=True):
+                 tile_shape=None, keep_images=False, plain=False, range64=True, batch_pixels=512 * 512):
         """``volumes``: name -> (bricks, kdtree or None); ``tfs``: name ->
         transfer function.  ``plain``: one single-view launch per request
         on one stream (``slots`` and ``max_batch`` are then 1).
@@ -114,7 +119,11 @@ class RenderServer:
         transfer-function bound is kept or dropped as yt's float64 test
         decides (field_interpolation_tables.pxd:72-73) -- a transfer
         function whose bounds lie inside the data's range otherwise drops or
-        keeps a few such samples differently."""
+        keeps a few such samples differently.
+        ``batch_pixels``: requests with fewer pixels go into the persistent
+        batch kernel together; larger ones, which fill the GPU on their own
+        (512^2 pixels are 2048 tiles, several waves), take the single-view
+        kernel one after another on the launch's stream."""
         self.device = torch.device(device)
         self.plain = bool(plain)
         if self.plain:
@@ -140,6 +149,7 @@ class RenderServer:
         self.max_batch = max_batch
         self.tile_shape = tile_shape
         self.keep_images = keep_images
+        self.batch_pixels = int(batch_pixels)
         self.samples = 0
         self.cancelled = []
         self.on_tick = None   # test hook: called with (server, now) once per loop turn
@@ -156,33 +166,53 @@ class RenderServer:
         return r
 
     def _launch(self, reqs, stream, now):
-        # a batch of one renders through the single-view kernel (which
-        # stages its table in shared memory and needs no work queue); the
-        # persistent batch kernel pays off from two views on
+        """Launch a group of requests on one stream: the small ones (under
+        batch_pixels) in one persistent batch launch first, then the large
+        ones -- and a lone small one -- each through the single-view kernel
+        (which stages its table in shared memory and needs no work queue),
+        with a completion event after each launch so that every request
+        finishes when its own launch does."""
         for q in reqs:
             q.batch_size = len(reqs)
-        if self.plain or len(reqs) == 1:
-            return self._launch_plain(reqs, stream, now)
-        jobs = []
-        for q in reqs:
-            q.image = torch.empty((*q.camera.resolution, 4), dtype=torch.float64, device=self.device)
-            r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
-            jobs.append(Job(r, q.camera, q.kind, q.n_samples, q.image))
-        b = Batch(jobs, device=self.device, tile_shape=self.tile_shape)
+        f = _InFlight([], stream, sum(q.image_bytes for q in reqs), [], [])
         stream.wait_stream(torch.cuda.current_stream(self.device))
-        b.launch(stream)
-        ev = torch.cuda.Event()
-        ev.record(stream)
-        for q in reqs:
-            q.launched = now
-        return _InFlight(reqs, ev, stream, sum(q.image_bytes for q in reqs), b.counters, b.error, [b])
+        if self.plain:
+            self._launch_plain(reqs, stream, now, f)
+            return f
+        small = [q for q in reqs if q.pixels < self.batch_pixels]
+        large = [q for q in reqs if q.pixels >= self.batch_pixels]
+        if len(small) == 1:
+            large = small + large
+            small = []
+        if small:
+            jobs = []
+            for q in small:
+                q.image = torch.empty((*q.camera.resolution, 4), dtype=torch.float64, device=self.device)
+                r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
+                jobs.append(Job(r, q.camera, q.kind, q.n_samples, q.image))
+            b = Batch(jobs, device=self.device, tile_shape=self.tile_shape)
+            b.launch(stream)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            for q in small:
+                q.launched = now
+            f.parts.append((small, ev))
+            f.counters.append(b.counters)
+            f.errors.append(b.error)
+            f.keep.append(b)
+        if large:
+            self._launch_plain(large, stream, now, f)
+        return f
 
-    def _launch_plain(self, reqs, stream, now):
+    def _launch_plain(self, reqs, stream, now, f):
+        """Each request through the single-view kernel on ``stream``, one
+        completion event per request, into the in-flight record ``f``."""
         from .volume import render as vrender
 
         pl = _Plain(self.device)
-        keep = []
-        stream.wait_stream(torch.cuda.current_stream(self.device))
+        f.counters.append(pl.counters)
+        f.errors.append(pl.error)
+        keep = f.keep
         for q in reqs:
             r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
             with torch.cuda.stream(stream):
@@ -195,9 +225,9 @@ class RenderServer:
                     n_samples=q.n_samples, flags=int(ts) << _lib.FLAG_TILE_SHIFT, counters=pl.counters,
                     error=pl.error, stream=stream, keep=keep)
             q.launched = now
-        ev = torch.cuda.Event()
-        ev.record(stream)
-        return _InFlight(reqs, ev, stream, sum(q.image_bytes for q in reqs), pl.counters, pl.error, keep)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            f.parts.append(([q], ev))
 
     def run(self, requests, realtime=True, timeout=600.0):
         """Serve ``requests`` (sorted by arrival).  With ``realtime`` the
@@ -223,20 +253,24 @@ class RenderServer:
                 self.in_use -= q.image_bytes
                 q.done = now
                 self.cancelled.append(q)
-            # retire finished batches
+            # retire finished launches (a group's launches end in stream order);
+            # a group frees its slot and budget when its last launch ends
             for f in list(inflight):
-                if f.event.query():
+                while f.parts and f.parts[0][1].query():
+                    part, _ = f.parts.pop(0)
                     t = time.perf_counter() - t0
-                    for q in f.requests:
+                    for q in part:
                         q.done = t
                         keep = self.keep_images(q) if callable(self.keep_images) else self.keep_images
                         if not keep:
                             q.image = None
+                    done += part
+                if not f.parts:
                     self.in_use -= f.bytes
-                    self.samples += int(f.counters[0].item())
-                    _lib.check(_lib.lib().ytgb_check_error(f.error.data_ptr(), f.stream.cuda_stream), "serve")
+                    for c, e in zip(f.counters, f.errors):
+                        self.samples += int(c[0].item())
+                        _lib.check(_lib.lib().ytgb_check_error(e.data_ptr(), f.stream.cuda_stream), "serve")
                     inflight.remove(f)
-                    done += f.requests
             if self.on_tick is not None:
                 self.on_tick(self, now)
             # admit arrivals within the HBM budget
