@@ -105,6 +105,11 @@ typedef struct ytgb_view {
     double camera_data[15];   /* position, width, east, north, normal */
     double pdx, pdy;          /* (bounds[1]-bounds[0])/nx, (bounds[3]-bounds[2])/ny */
     double ray_scale;         /* perspective: max_length / width[2] (lens.py:204-211) */
+    /* derived by the library from the fields above before each launch and in
+     * ytgb_batch_plan (callers need not set them): the perspective lens's
+     * linspace steps 1/(nx-1), 1/(ny-1) (0 for one pixel) and normal * width[2] */
+    double lin_step[2];
+    double normal_w2[3];
     const double *px_pos;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
     const double *px_dir;     /* device (nx,ny,3) for YTGB_LENS_PER_PIXEL, else NULL */
 } ytgb_view;

@@ -51,8 +51,11 @@ static void run(const ytgb_render_args &a, unsigned long long *hashes, long long
         }
 }
 
-extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long long *hashes, long long *counts,
+extern "C" int emu_render(const ytgb_render_args *a_in, int trace, unsigned long long *hashes, long long *counts,
                           unsigned long long *cnt) {
+    ytgb_render_args copy = *a_in;  // the launch's derived view constants, as ytgb_render forms them
+    view_derive(copy.view);
+    const ytgb_render_args *a = &copy;
     if (trace) { run<MODE_TRACE, 0>(*a, hashes, counts, cnt); return 0; }
     switch (a->kind) {
     case YTGB_VOLUME_RENDER:
@@ -75,7 +78,10 @@ extern "C" int emu_render(const ytgb_render_args *a, int trace, unsigned long lo
 }
 
 // the rays make_ray generates for every pixel (positions and directions)
-extern "C" void emu_rays(const ytgb_view *v, double *pos, double *dir) {
+extern "C" void emu_rays(const ytgb_view *v_in, double *pos, double *dir) {
+    ytgb_view vd = *v_in;
+    view_derive(vd);
+    const ytgb_view *v = &vd;
     for (int vi = 0; vi < v->nx; vi++)
         for (int vj = 0; vj < v->ny; vj++) {
             Ray r;
@@ -216,8 +222,11 @@ static int run_octree(const ytgb_render_args &a, const ytgb_octree_args &oa, uns
     return bad;
 }
 
-extern "C" int emu_octree(const ytgb_render_args *a, const ytgb_octree_args *o, int trace,
+extern "C" int emu_octree(const ytgb_render_args *a_in, const ytgb_octree_args *o, int trace,
                           unsigned long long *hashes, long long *counts, unsigned long long *cnt) {
+    ytgb_render_args copy = *a_in;
+    view_derive(copy.view);
+    const ytgb_render_args *a = &copy;
     if (trace) return run_octree<MODE_TRACE, 0>(*a, *o, hashes, counts, cnt);
     switch (a->kind) {
     case YTGB_VOLUME_RENDER:

@@ -63,6 +63,8 @@ class View(C.Structure):
         ("pdx", C.c_double),
         ("pdy", C.c_double),
         ("ray_scale", C.c_double),
+        ("lin_step", C.c_double * 2),
+        ("normal_w2", C.c_double * 3),
         ("px_pos", C.c_void_p),
         ("px_dir", C.c_void_p),
     ]

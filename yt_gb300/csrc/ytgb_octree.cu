@@ -172,7 +172,9 @@ int octree_launch(const ytgb_render_args *a, const ytgb_octree_args *o, size_t s
         ytgb_set_error("ytgb_render_octree: image too large");
         return YTGB_ERR_INVALID;
     }
-    octree_kernel<MODE, CTF><<<(unsigned)blocks, OBLOCK, smem, s>>>(*a, *o, h, c);
+    ytgb_render_args b = *a;
+    view_derive(b.view);
+    octree_kernel<MODE, CTF><<<(unsigned)blocks, OBLOCK, smem, s>>>(b, *o, h, c);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         ytgb_set_error(std::string("octree launch: ") + cudaGetErrorString(e));

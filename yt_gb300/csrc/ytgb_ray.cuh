@@ -247,6 +247,15 @@ struct Ray {
     double td_dds[3], td[3];
 };
 
+// The view's derived per-view constants (host, before a launch): the
+// perspective lens's linspace steps and normal * width[2], the same float64
+// operations make_ray would repeat per pixel.
+inline void view_derive(ytgb_view &v) {
+    v.lin_step[0] = v.nx > 1 ? 1.0 / (double)(v.nx - 1) : 0.0;
+    v.lin_step[1] = v.ny > 1 ? 1.0 / (double)(v.ny - 1) : 0.0;
+    for (int i = 0; i < 3; i++) v.normal_w2[i] = v.vp_pos[9 + i] * v.vp_dir[2];
+}
+
 // generate_vector_info_plane_parallel (lenses.pyx:179-192) and
 // generate_vector_info_null (lenses.pyx:196-207)
 YTGB_HD void make_ray(const ytgb_view &v, int vi, int vj, Ray &r) {
@@ -262,17 +271,14 @@ YTGB_HD void make_ray(const ytgb_view &v, int vi, int vj, Ray &r) {
         // PerspectiveLens._get_sampler_params (lens.py:186-225) for one pixel:
         // px = linspace(-0.5, 0.5, nx)[vi] (numpy: i*step + start, last = stop),
         // vector = (w0*(east*px) + w1*(north*py) + normal*w2) * (max_length/w2)
-        const double px = (v.nx > 1 && vi == v.nx - 1)
-                              ? 0.5
-                              : dadd(dmul((double)vi, v.nx > 1 ? ddiv(1.0, (double)(v.nx - 1)) : 0.0), -0.5);
-        const double py = (v.ny > 1 && vj == v.ny - 1)
-                              ? 0.5
-                              : dadd(dmul((double)vj, v.ny > 1 ? ddiv(1.0, (double)(v.ny - 1)) : 0.0), -0.5);
+        // (lin_step and normal_w2: view_derive, once per view)
+        const double px = (v.nx > 1 && vi == v.nx - 1) ? 0.5 : dadd(dmul((double)vi, v.lin_step[0]), -0.5);
+        const double py = (v.ny > 1 && vj == v.ny - 1) ? 0.5 : dadd(dmul((double)vj, v.lin_step[1]), -0.5);
         YTGB_UNROLL
         for (int i = 0; i < 3; i++) {
             const double sx = dmul(v.vp_dir[0], dmul(v.vp_pos[3 + i], px));
             const double sy = dmul(v.vp_dir[1], dmul(v.vp_pos[6 + i], py));
-            r.dir[i] = dmul(dadd(dadd(sx, sy), dmul(v.vp_pos[9 + i], v.vp_dir[2])), v.ray_scale);
+            r.dir[i] = dmul(dadd(dadd(sx, sy), v.normal_w2[i]), v.ray_scale);
             r.pos[i] = v.vp_pos[i];
         }
     } else {
@@ -1133,9 +1139,15 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, Ray &r, 
     const ytgb_tf &tf = a.tf;
     const float nbm2 = (float)(tf.nbins[0] - 2);
     const bool grey = GREY >= 0 ? GREY == 1 : tf.grey_opacity == 1;
+    // The cell-value samplers (projection, MIP) run integer-pipe bound: for
+    // them the step bound is tested with the exit test, a tie in the tmax
+    // step takes the float64 add, and the exit test checks all three indices
+    // instead of selecting the stepped one (7-12 % faster there; the
+    // interpolating samplers measured slower with it).
+    constexpr bool CELLS = MODE == MODE_PROJ || MODE == MODE_MIP;
     unsigned nv = 0;
     while (true) {
-        if (nv >= (unsigned)step_limit) {
+        if (!CELLS && nv >= (unsigned)step_limit) {
             set_error(a.error, YTGB_DEVERR_STEP_LIMIT);
             break;
         }
@@ -1228,12 +1240,13 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, Ray &r, 
         const int md = s0 ? A0.mode : (s1 ? A1.mode : A2.mode);
         const int ex = s0 ? A0.ex : (s1 ? A1.ex : A2.ex);
         long long nb = tmb + inc;
-        if (md == 2) nb += nb & 1;  // a tie: to the even neighbour
+        if (!CELLS && md == 2) nb += nb & 1;  // a tie: to the even neighbour
         A0.bits = s0 ? nb : A0.bits;
         A1.bits = s1 ? nb : A1.bits;
         A2.bits = s2 ? nb : A2.bits;
-        if (md == 3 || (int)(nb >> 52) != ex) {
-            // tmax leaves its binade (or has no integer step): the float64 add
+        if ((CELLS ? md >= 2 : md == 3) || (int)(nb >> 52) != ex) {
+            // tmax leaves its binade, or has no integer step (or, CELLS, its
+            // step rounds a tie to even): the float64 add
             // (the ray is in shared memory: a runtime index costs no local memory)
             const int i = s0 ? 0 : (s1 ? 1 : 2);
             const double td = r.td[i];  // (kept by the prologue for this brick)
@@ -1250,9 +1263,20 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, Ray &r, 
             }
         }
         eb = tmb;
-        const int ci = s0 ? c0 : (s1 ? c1 : c2);
-        const int dci = s0 ? c.dims[0] : (s1 ? c.dims[1] : c.dims[2]);
-        if ((unsigned)ci >= (unsigned)dci || !(tmb < kmax)) break;  // ... or enter_t >= max_t
+        if (CELLS) {
+            // the stepped index left the brick (the others did not change), or
+            // enter_t >= max_t; or the walk's step bound was reached
+            const bool out = (unsigned)c0 >= (unsigned)c.dims[0] || (unsigned)c1 >= (unsigned)c.dims[1] ||
+                             (unsigned)c2 >= (unsigned)c.dims[2] || !(tmb < kmax);
+            if (out || nv >= (unsigned)step_limit) {
+                if (!out) set_error(a.error, YTGB_DEVERR_STEP_LIMIT);
+                break;
+            }
+        } else {
+            const int ci = s0 ? c0 : (s1 ? c1 : c2);
+            const int dci = s0 ? c.dims[0] : (s1 ? c.dims[1] : c.dims[2]);
+            if ((unsigned)ci >= (unsigned)dci || !(tmb < kmax)) break;  // ... or enter_t >= max_t
+        }
     }
     st.visits += nv;
     if (nv) {

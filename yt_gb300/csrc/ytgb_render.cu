@@ -394,7 +394,9 @@ int launch(const ytgb_render_args *a, size_t smem, cudaStream_t s, unsigned long
         return YTGB_ERR_INVALID;
     }
     if (int st = set_smem(render_kernel<MODE, VAR, TS>, smem)) return st;
-    render_kernel<MODE, VAR, TS><<<grid, BLOCK, smem, s>>>(*a, h, c);
+    ytgb_render_args b = *a;
+    view_derive(b.view);
+    render_kernel<MODE, VAR, TS><<<grid, BLOCK, smem, s>>>(b, h, c);
     return launch_status("render launch");
 }
 
@@ -508,6 +510,7 @@ extern "C" int ytgb_batch_plan(ytgb_batch_entry *entries, int32_t n, int32_t til
     for (int32_t k = 0; k < n; k++) {
         ytgb_render_args &a = entries[k].args;
         if (int st = check_args(&a, false)) return st;
+        view_derive(a.view);
         if (a.kind != kind || render_variant(a) != var) {
             ytgb_set_error("ytgb_batch_plan: every entry of a batch must use the same sampler, table layout and "
                            "range decisions (data_lo with range_eps > 0, or neither)");
@@ -671,6 +674,13 @@ int noalloc_check_plan(const ytgb_batch_entry *h, int32_t n, int32_t kind, int32
             smem = sm > smem ? sm : smem;
         }
         const long long tx = (a.view.nx + TX - 1) / TX, ty = (a.view.ny + TY - 1) / TY;
+        ytgb_view dv = a.view;
+        view_derive(dv);
+        if (std::memcmp(&dv, &a.view, sizeof(dv)) != 0) {
+            ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
+                           " has no derived view constants (run ytgb_batch_plan on the table)");
+            return YTGB_ERR_INVALID;
+        }
         if (h[k].tile_begin != total || h[k].tiles_y != ty || h[k].tiles != tx * ty) {
             ytgb_set_error("ytgb_batch_render_noalloc: entry " + std::to_string(k) +
                            " is not planned for this tile shape (run ytgb_batch_plan with it)");
