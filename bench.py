@@ -1028,9 +1028,14 @@ def run_octree(args):
     gimg = torch.zeros((cres, cres, 4), dtype=torch.float64, device=dev)
     render_octree(vol, ccam.device_view(), _lib.VOLUME_RENDER, gimg, tf=packed)
     mx, rms = relative_error(gimg.cpu().numpy(), p["image"], channels=(0, 1, 2))
+    hbm, _ = peaks()
+    alg = samples * BYTES_PER_SAMPLE + res * res * BYTES_PER_RAY
     line = {"metric": "Gsamples/s", "workload": "octree", "value": samples / (ms.mean() / 1e3) / 1e9,
             "unit": "Gsamples/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
             "ms_per_step": float(ms.mean()), "higher_is_better": True, "samples_per_step": samples,
+            "roofline": {"bound": "hbm", "achieved": alg / (float(ms.mean()) / 1e3) / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": alg / (float(ms.mean()) / 1e3) / 1e9 / hbm,
+                         "model": f"{BYTES_PER_SAMPLE} B/sample + {BYTES_PER_RAY} B/ray (the kd path's model)"},
             "cpu_baseline": {**cpu, "unit": "Gsamples/s", "cores": threads,
                              "sample": f"the same camera at {cres}x{cres} ({cvis} samples)"},
             "accuracy": {"max_rel_err": mx, "rms_rel_err": rms, "vs": f"float64 oracle at {cres}x{cres}"},
