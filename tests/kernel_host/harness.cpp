@@ -150,6 +150,8 @@ extern "C" long long emu_check_convert(long long n, unsigned long long seed) {
         float got = diff_to_float(dbits(x), dbits(y));
         long double exact = (long double)x - (long double)y;
         if (!within_ulp(got, exact)) bad++;
+        // the cell loop's form gives the same value
+        if (diff_to_float_loop(dbits(x), dbits(y)) != got) bad++;
         double t = std::ldexp((double)(g() >> 11), -(int)(g() % 60));  // 0 <= t < 2^53 .. small
         if (t > 0 && t < 1073741824.0) {
             int fl; float fr;

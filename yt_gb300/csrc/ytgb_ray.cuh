@@ -175,6 +175,27 @@ YTGB_HD float diff_to_float(long long xb, long long yb) {
     return xb >= yb ? diff_to_float_ordered(xb, yb) : -diff_to_float_ordered(yb, xb);
 }
 
+// x - y as float in the cell loop: when both lie in one binade inside the
+// scaled conversion's range (the loop's case: 2^-74 <= t < 2^74) and
+// x >= y, the difference in ulps converted as scaled_to_float_fast does,
+// with one test instead of diff_to_float's three; otherwise diff_to_float.
+// The same value as diff_to_float.
+YTGB_HD float diff_to_float_loop(long long xb, long long yb) {
+    const unsigned xh = (unsigned)((unsigned long long)xb >> 32), yh = (unsigned)((unsigned long long)yb >> 32);
+    const long long F = xb - yb;
+    const unsigned ex = xh >> 20;  // the sign and exponent fields
+    if ((xh ^ yh) < (1u << 20) && F >= 0 && ex - 949u <= 199u) {
+        const unsigned hi = (unsigned)((unsigned long long)F >> 32), lo = (unsigned)F;
+#ifdef __CUDA_ARCH__
+        const float f = ffma(__uint2float_rn(hi), 4294967296.0f, __uint2float_rn(lo));
+#else
+        const float f = ffma((float)hi, 4294967296.0f, (float)lo);
+#endif
+        return fmul(f, ffrom((ex - 948u) << 23));  // 2^(ex - 1075)
+    }
+    return diff_to_float(xb, yb);
+}
+
 // floor(ty) and ty - floor(ty) (as float) for a positive normal ty < 2^30.
 YTGB_HD void split_floor(long long tb, int &fl, float &frac) {
     const int e = (int)(tb >> 52) - 1023;
@@ -1159,7 +1180,7 @@ YTGB_HD void cells_fast(const ytgb_render_args &a, const float4 *s_tab, Ray &r, 
         const bool s2 = !s0 && !s1;
         const long long tmb = s0 ? A0.bits : (s1 ? A1.bits : A2.bits);
         const long long xb = tmb < kmax ? tmb : kmax;  // fmin(tmax[i], max_t)
-        const float dtf = diff_to_float(xb, eb);
+        const float dtf = diff_to_float_loop(xb, eb);
         // the sample at the middle of the cell's segment (n_samples = 1)
         const float f = fmul(dtf, 0.5f);
         const float fx = cell_coord<true>(ffma(f, v0, P0));
