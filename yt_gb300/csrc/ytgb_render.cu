@@ -71,7 +71,10 @@ constexpr int NWARP = BLOCK / 32;
 // 1.199 ms against 1.234 ms at 5 (96 registers, no spills), and the
 // projections 3-6 % faster.  The persistent batch kernel, whose loop keeps
 // more state, takes 5: the 64-view batch runs 32.7 ms against 33.2 ms at
-// 6.  Images are identical at every setting.  YTGB_MIN_BLOCKS sets both
+// 6.  The single-view kernel's float64-range-decision variants (V_REF, the
+// served form's) keep 5 too: at 80 registers their rare float64 path
+// spilled ~1 KB a thread and the served frame ran 2.46 ms against 2.03 ms
+// at 96.  Images are identical at every setting.  YTGB_MIN_BLOCKS sets both
 // (a second build at another budget, for the bit-identity test).
 #ifdef YTGB_MIN_BLOCKS
 constexpr int MIN_BLOCKS = YTGB_MIN_BLOCKS, BATCH_MIN_BLOCKS = YTGB_MIN_BLOCKS;
@@ -200,7 +203,7 @@ __device__ __forceinline__ void warp_tile(const ytgb_render_args &a, int bx, int
 
 // One view, one tile per block (four warps of 32 pixels).
 template <int MODE, int VAR, int TS>
-__global__ void __launch_bounds__(BLOCK, MIN_BLOCKS) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
+__global__ void __launch_bounds__(BLOCK, (VAR & V_REF) ? BATCH_MIN_BLOCKS : MIN_BLOCKS) render_kernel(const ytgb_render_args a, unsigned long long *hashes,
                                                        long long *counts) {
     extern __shared__ float4 s_tab[];
     __shared__ TileSmem sm;
