@@ -17,15 +17,18 @@
 //   * comparisons of walk values use order-preserving int64 keys;
 //   * per cell `tmax += tdelta` runs as an integer add on the bit pattern
 //     (float64 only when tmax leaves its binade) and `exit_t - enter_t` as
-//     an integer difference converted to float32 once;
+//     an integer difference converted to float32 once, by 32-bit integer
+//     conversions (a 64-bit conversion runs on the float64 pipe);
 //   * the sample position is tracked in float32, in cell-local coordinates
 //     reset exactly on the axis the walk steps along;
 //   * bricks a ray clearly misses, faces it clearly does not enter through,
 //     and start points clearly outside a brick are rejected by float32 tests
 //     whose margins exceed their float32 error by orders of magnitude, before
 //     the exact float64 tests;
-//   * the per-walk state is kept small enough to stay in registers at 20
-//     warps per SM (tdelta is recomputed per walk rather than cached).
+//   * the per-walk state is kept small (the rays themselves live in shared
+//     memory, each ray keeps its tdelta products for the last brick's cell
+//     width there, and the per-view constants of the perspective rays are
+//     formed once on the host).
 // Sampling (trilinear, transfer function) runs in float32 on float32 brick
 // data.  The image accumulates as a float32 value plus a float32 error term
 // with error-free transformations (TwoSum, Knuth; TwoProduct via FMA), so
