@@ -1,6 +1,7 @@
 """Host logic of the render server, without a GPU: the priority level of
 each launch (first come, first served among batches in flight)."""
-from yt_gb300.serve import PRIORITY_LEVELS, launch_level
+from yt_gb300.camera import Camera
+from yt_gb300.serve import PRIORITY_LEVELS, Request, launch_level, split_group
 
 
 def test_launch_level_is_below_every_batch_in_flight():
@@ -12,3 +13,19 @@ def test_launch_level_is_below_every_batch_in_flight():
     assert launch_level([PRIORITY_LEVELS - 1]) == PRIORITY_LEVELS - 1
     # an idle GPU starts again at the top
     assert launch_level(iter(())) == 0
+
+
+def _req(i, res):
+    return Request(i, "v", "t", Camera((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 1.0, res), arrival=0.01 * i)
+
+
+def test_split_group_batches_only_small_requests():
+    reqs = [_req(0, 256), _req(1, 2048), _req(2, 256), _req(3, 512), _req(4, 128)]
+    small, large = split_group(reqs, 512 * 512)
+    assert [q.rid for q in small] == [0, 2, 4] and [q.rid for q in large] == [1, 3]
+    # a lone small request takes the single-view kernel, first
+    small, large = split_group([_req(0, 2048), _req(1, 256)], 512 * 512)
+    assert small == [] and [q.rid for q in large] == [1, 0]
+    # 0 batches nothing; a huge threshold batches everything
+    assert split_group(reqs, 0)[0] == []
+    assert len(split_group(reqs, 1 << 30)[0]) == 5

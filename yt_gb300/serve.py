@@ -81,6 +81,17 @@ class Request:
 PRIORITY_LEVELS = 4  # stream priorities the served launches use (0 .. -3)
 
 
+def split_group(reqs, batch_pixels: int):
+    """A launch group's requests as (batched, alone): the small ones (under
+    ``batch_pixels`` pixels) share one persistent batch launch; the large
+    ones -- and a lone small one -- take the single-view kernel each."""
+    small = [q for q in reqs if q.pixels < batch_pixels]
+    large = [q for q in reqs if q.pixels >= batch_pixels]
+    if len(small) == 1:
+        return [], small + large
+    return small, large
+
+
 def launch_level(levels_in_flight) -> int:
     """The priority level of a new launch (0 the highest): one below every
     batch still in flight, the lowest level once that is reached."""
@@ -179,11 +190,7 @@ class RenderServer:
         if self.plain:
             self._launch_plain(reqs, stream, now, f)
             return f
-        small = [q for q in reqs if q.pixels < self.batch_pixels]
-        large = [q for q in reqs if q.pixels >= self.batch_pixels]
-        if len(small) == 1:
-            large = small + large
-            small = []
+        small, large = split_group(reqs, self.batch_pixels)
         if small:
             jobs = []
             for q in small:
