@@ -186,7 +186,6 @@ class RenderServer:
         for q in reqs:
             q.batch_size = len(reqs)
         f = _InFlight([], stream, sum(q.image_bytes for q in reqs), [], [])
-        stream.wait_stream(torch.cuda.current_stream(self.device))
         if self.plain:
             self._launch_plain(reqs, stream, now, f)
             return f
@@ -198,6 +197,9 @@ class RenderServer:
                 r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
                 jobs.append(Job(r, q.camera, q.kind, q.n_samples, q.image))
             b = Batch(jobs, device=self.device, tile_shape=self.tile_shape)
+            # the batch's tables, counters and error word were written on
+            # the current stream
+            stream.wait_stream(torch.cuda.current_stream(self.device))
             b.launch(stream)
             ev = torch.cuda.Event()
             ev.record(stream)
@@ -219,6 +221,8 @@ class RenderServer:
         pl = _Plain(self.device)
         f.counters.append(pl.counters)
         f.errors.append(pl.error)
+        # the counters and error word were zeroed on the current stream
+        stream.wait_stream(torch.cuda.current_stream(self.device))
         keep = f.keep
         for q in reqs:
             r = self.renderer(q.volume, q.tf if q.kind == _lib.VOLUME_RENDER else None)
