@@ -221,3 +221,38 @@ def test_light_source_drop_in(cuda):
     ref, *_ = oracle_render(w.bricks, cam, order, _lib.LIGHT_SOURCE, tf=w.tf, n_samples=2,
                             light=((0.2, -1.0, 0.5), (1.0, 0.8, 0.6, 1.0)))
     assert relative_error(img, ref, channels=(0, 1, 2))[0] <= TOL
+
+
+@pytest.mark.parametrize("res", [(1, 1), (1, 7), (9, 1)])
+@pytest.mark.parametrize("lens", ["perspective", "plane-parallel"])
+def test_degenerate_images(cuda, res, lens):
+    """One-pixel rows and columns (the perspective lens's per-view linspace
+    step is 0 there, the plane-parallel lens divides by zero as yt does):
+    walk, visit count and image as the oracle's, NaN pixels included."""
+    w = workloads.uniform_vr(n=12, res=8)
+    cam = Camera((0.45, 0.55, -1.0), (0.5, 0.5, 0.5), 1.0, res, lens_type=lens)
+    r = Renderer(w.bricks, w.tf, device=cuda, kdtree=w.kdtree)
+    order = r.order(cam)
+    r.counters.zero_()
+    img = r.render(cam, order=order).cpu().numpy()
+    r.check()
+    ref, visits, h_ref, c_ref = oracle_render(w.bricks, cam, order, _lib.VOLUME_RENDER, tf=w.tf)
+    assert np.array_equal(np.isnan(img), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert np.allclose(img[ok], ref[ok], rtol=TOL, atol=1e-12)
+    assert int(r.counters[0].item()) == visits
+    h, c = r.trace(cam, order)
+    assert np.array_equal(c, c_ref) and np.array_equal(h, h_ref)
+
+
+def test_empty_brick_list(cuda):
+    """An empty order renders nothing: the image is left as it was."""
+    import torch
+
+    w = workloads.uniform_vr(n=8, res=8)
+    cam = Camera((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 1.0, 8)
+    r = Renderer(w.bricks, w.tf, device=cuda)
+    start = torch.full((8, 8, 4), 0.25, dtype=torch.float64, device=cuda)
+    img = r.render(cam, order=np.zeros(0, dtype=np.int32), image=start.clone())
+    r.check()
+    assert torch.equal(img, start)

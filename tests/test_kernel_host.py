@@ -185,6 +185,30 @@ def test_grey_opacity_and_multivariate(emu):
     check(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=mv)
 
 
+@pytest.mark.parametrize("res", [(1, 1), (1, 7), (9, 1)])
+@pytest.mark.parametrize("lens", ["perspective", "plane-parallel"])
+def test_degenerate_images(emu, res, lens):
+    """One-pixel rows and columns: the perspective lens's linspace of one
+    point is its start (-0.5), the plane-parallel lens's pixel position
+    divides by zero as yt's does; walk and image as the oracle's."""
+    w = workloads.uniform_vr(n=12, res=8)
+    cam = Camera((0.45, 0.55, -1.0), (0.5, 0.5, 0.5), 1.0, res, lens_type=lens)
+    img, cnt, h, c = run_emu(emu, w.bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=w.tf)
+    ref, visits, hr, cr = run_oracle(w.bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf=w.tf)
+    assert np.array_equal(np.isnan(img), np.isnan(ref))
+    assert np.array_equal(c, cr) and np.array_equal(h, hr) and int(cnt[0]) == visits
+    ok = ~np.isnan(ref)
+    assert np.allclose(img[ok], ref[ok], rtol=1e-5, atol=1e-12)
+
+
+def test_empty_brick_list(emu):
+    """No bricks in the order: no walk, the image as it was."""
+    w = workloads.uniform_vr(n=8, res=8)
+    cam = Camera((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 1.0, 8)
+    img, cnt, h, c = run_emu(emu, w.bricks, cam, np.zeros(0, dtype=np.int32), _lib.VOLUME_RENDER, tf=w.tf)
+    assert not img.any() and int(cnt[0]) == 0 and int(cnt[1]) == 0 and not c.any()
+
+
 def near_bound_case(n=8, seed=3):
     """One brick whose every vertex value lies within 1e-9 of b = 1 + 2^-30,
     the upper bound of the transfer functions below: float32 has no value
