@@ -123,3 +123,14 @@ def test_plan_asks_for_shared_memory_only_for_one_shared_table():
     assert sm.value == 0 and t.value == total
     st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
     assert st == _lib.ERR_INVALID and "different" in msg
+
+
+def test_noalloc_rejects_views_without_derived_constants():
+    """ytgb_batch_plan derives each view's per-view ray constants (the
+    perspective lens's linspace steps and normal * width); a table that did
+    not go through it is rejected before anything is queued."""
+    entries, n, total, smem, ctf = planned()
+    assert entries[0].args.view.lin_step[0] > 0
+    entries[1].args.view.lin_step[0] = 0.0
+    st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
+    assert st == _lib.ERR_INVALID and "derived view constants" in msg
