@@ -352,3 +352,25 @@ def test_native_offaxis_stamp_matches_numpy():
         s1, m1 = offaxis.offaxis_stamp(rot, dxm, n, n)
         s2, m2 = offaxis.offaxis_stamp(rot, dxm, n, n, native=False)
         assert np.array_equal(s1.view(np.int64), s2.view(np.int64)) and np.array_equal(m1, m2)
+
+
+def test_range_eps_is_the_largest_finite_value():
+    """BrickSet(with_lo=True).range_eps = 2^-24 * the largest finite |value|
+    of the arena (NaN and infinite values excluded, the padding between
+    fields zeroed); 0 without the rounding errors."""
+    from yt_gb300.volume import BrickSet
+
+    rng = np.random.default_rng(2)
+    a = rng.normal(0.0, 3.0, (5, 5, 5))
+    b = rng.normal(0.0, 1.0, (3, 4, 6))
+    a[0, 0, 0], a[1, 1, 1], b[0, 0, 0] = np.nan, np.inf, -np.inf
+    bricks = [([a], None, np.zeros(3), np.ones(3), np.array([4, 4, 4])),
+              ([b], None, np.zeros(3), np.ones(3), np.array([2, 3, 5]))]
+    bs = BrickSet(bricks, device="cpu", with_lo=True)
+    finite = np.concatenate([a[np.isfinite(a)], b[np.isfinite(b)]]).astype(np.float32)
+    assert bs.range_eps == float(np.abs(finite).max()) * 2.0 ** -24
+    assert BrickSet(bricks, device="cpu").range_eps == 0.0
+    bs.data[0] = 1e30
+    assert bs.range_eps == float(np.abs(finite).max()) * 2.0 ** -24  # kept until data_changed()
+    bs.data_changed()
+    assert bs.range_eps == float(np.float32(1e30)) * 2.0 ** -24
