@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--audit", type=int, default=20, help="requests re-rendered by the oracle (--workload serve)")
     ap.add_argument("--no-batched", action="store_true", help="default line without the batched record")
     ap.add_argument("--no-served", action="store_true", help="default line without the served record")
-    ap.add_argument("--served-requests", type=int, default=100, help="requests per rate in the default line")
+    ap.add_argument("--served-requests", type=int, default=200, help="requests per rate in the default line")
     ap.add_argument("--max-batch", type=int, default=64, help="requests per served batch (--workload serve)")
     ap.add_argument("--slots", type=int, default=4, help="streams of the render server (--workload serve)")
     ap.add_argument("--batch-pixels", type=int, default=512 * 512,
