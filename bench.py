@@ -780,6 +780,15 @@ def serve_requests(vols, n, rate, seed):
     return out
 
 
+def p99_flags(served, plain):
+    """Whether the served form's p99 is at or below the plain form's, and
+    whether the run tells the two apart at all (their bootstrap 95 %
+    intervals overlap or not)."""
+    sc, pc = served["p99_ci95_ms"], plain["p99_ci95_ms"]
+    return {"served_beats_plain_p99": served["p99_ms"] <= plain["p99_ms"],
+            "p99_intervals_overlap": sc[0] <= pc[1] and pc[0] <= sc[1]}
+
+
 def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slots=4, batch_pixels=512 * 512):
     """Served rendering against plain: at each rate the same Poisson stream
     goes through the render server (HBM-budget admission, continuous
@@ -816,7 +825,7 @@ def serve_record(dev, n_requests, rates, audit=None, amr=None, max_batch=64, slo
                               "samples": server.samples}
                 if label == "served":
                     audit_set += [q for q in done if q.rid % 100 == 0]
-            row["served_beats_plain_p99"] = row["served"]["p99_ms"] <= row["plain"]["p99_ms"]
+            row.update(p99_flags(row["served"], row["plain"]))
             rows.append(row)
         closed = {}
         for label, server in (("served", srv), ("plain", plain_srv)):

@@ -29,3 +29,33 @@ def test_split_group_batches_only_small_requests():
     # 0 batches nothing; a huge threshold batches everything
     assert split_group(reqs, 0)[0] == []
     assert len(split_group(reqs, 1 << 30)[0]) == 5
+
+
+def test_latency_summary_p99_interval():
+    from yt_gb300.serve import latency_summary
+
+    reqs = []
+    for i, ms in enumerate(list(range(1, 200)) + [1000]):
+        q = _req(i, 64)
+        q.arrival, q.done = 0.0, ms / 1e3
+        reqs.append(q)
+    s = latency_summary(reqs)
+    assert s["n"] == 200 and abs(s["p50_ms"] - 100.5) < 1e-9
+    lo, hi = s["p99_ci95_ms"]
+    assert lo <= s["p99_ms"] <= hi and hi <= 1000.0
+
+
+def test_bench_p99_flags():
+    """The per-rate comparison bench.py writes from two latency summaries."""
+    import importlib.util
+    from pathlib import Path
+
+    spec = importlib.util.spec_from_file_location("bench", Path(__file__).resolve().parent.parent / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    a = {"p99_ms": 10.0, "p99_ci95_ms": [9.0, 12.0]}
+    b = {"p99_ms": 11.0, "p99_ci95_ms": [10.5, 13.0]}
+    c = {"p99_ms": 20.0, "p99_ci95_ms": [18.0, 25.0]}
+    assert bench.p99_flags(a, b) == {"served_beats_plain_p99": True, "p99_intervals_overlap": True}
+    assert bench.p99_flags(b, a) == {"served_beats_plain_p99": False, "p99_intervals_overlap": True}
+    assert bench.p99_flags(a, c) == {"served_beats_plain_p99": True, "p99_intervals_overlap": False}
