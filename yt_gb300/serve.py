@@ -323,6 +323,9 @@ def latency_summary(reqs, seed=0, resamples=1000):
     few hundred requests the p99 is one of the largest few latencies, and two
     forms whose intervals overlap are not told apart by the run."""
     lat = np.array([q.latency for q in reqs]) * 1e3
+    if lat.size == 0:
+        nan = float("nan")
+        return {"p50_ms": nan, "p99_ms": nan, "p99_ci95_ms": [nan, nan], "mean_ms": nan, "max_ms": nan, "n": 0}
     rng = np.random.default_rng(seed)
     boot = np.percentile(lat[rng.integers(0, lat.size, (resamples, lat.size))], 99, axis=1)
     lo, hi = np.percentile(boot, [2.5, 97.5])
