@@ -134,3 +134,31 @@ def test_noalloc_rejects_views_without_derived_constants():
     entries[1].args.view.lin_step[0] = 0.0
     st, msg = noalloc(entries, n, _lib.VOLUME_RENDER, ctf, 1, total, smem)
     assert st == _lib.ERR_INVALID and "derived view constants" in msg
+
+
+def test_render_variant_cases():
+    """The kernel variant a render's arguments call for (``render_variant``,
+    the host mirror of the library's): the ColorTransferFunction layout for
+    volume rendering only; float64 range decisions with data_lo and a
+    positive range_eps, for volume rendering and the light source, but not
+    for a ColorTransferFunction whose table excludes every value."""
+    from yt_gb300.transfer_functions import ProjectionTransferFunction
+
+    w = workloads.uniform_vr(n=8, res=8)
+    a = _lib.RenderArgs()
+    a.kind = _lib.VOLUME_RENDER
+    a.tf = pack(w.tf).header
+    assert _lib.render_variant(a) == _lib.VARIANT_CTF
+    a.data_lo, a.range_eps = FAKE, 1e-7
+    assert _lib.render_variant(a) == _lib.VARIANT_CTF | _lib.VARIANT_RANGE64
+    a.range_eps = 0.0
+    assert _lib.render_variant(a) == _lib.VARIANT_CTF
+    a.kind, a.range_eps = _lib.LIGHT_SOURCE, 1e-7
+    assert _lib.render_variant(a) == _lib.VARIANT_RANGE64
+    a.kind = _lib.PROJECTION
+    assert _lib.render_variant(a) == 0
+    # a table that excludes every value (all-zero table, bounds beyond float32)
+    a.kind = _lib.VOLUME_RENDER
+    a.tf = pack(ProjectionTransferFunction()).header
+    assert a.tf.lo_excl[0] > a.tf.hi_excl[0]
+    assert _lib.render_variant(a) & _lib.VARIANT_RANGE64 == (0 if a.tf.ctf_fast else _lib.VARIANT_RANGE64)
