@@ -31,9 +31,12 @@ tests do not depend on the synthetic generators staying bit-stable.
                 viewpoint order through a perspective camera
 * offaxis.npz   add_cells_to_image_offaxis (image_utilities.pyx:167-289):
                 octree cells splatted along oblique normals (offaxis_cases)
+* near_bound.npz VolumeRenderSampler on a field within 1e-9 of a
+                transfer-function bound float32 cannot represent (the
+                float64 range decisions), two cameras, 1 and 3 samples
 
-Pass fixture names (gz trace vr light octree proj kd offaxis) to make only
-those.
+Pass fixture names (gz trace vr light octree proj kd offaxis near_bound) to
+make only those.
 """
 from __future__ import annotations
 
@@ -130,6 +133,34 @@ def vr():
             s(PartitionedGrid(0, [v], np.ones((16, 16, 16), "uint8"), np.zeros(3), np.ones(3), dims), num_threads=1)
             out[f"img_{ci}_{ns}"] = np.array(s.aimage)
     np.savez_compressed(HERE / "vr.npz", **out)
+
+
+NB_CAMS = [((0.3, 0.6, -1.0), (1.5, 1.5, 1.5), (24, 24), "perspective"),
+           ((1.2, 0.3, -0.8), (1.0, 1.0, 1.0), (20, 24), "plane-parallel")]
+
+
+def near_bound():
+    """VolumeRenderSampler on a field whose every vertex value lies within
+    1e-9 of the upper bound b = 1 + 2^-30 of its ColorTransferFunction, a
+    value float32 cannot represent: yt's float64 test keeps the samples
+    below b and drops the others (field_interpolation_tables.pxd:72-73)."""
+    rng = np.random.default_rng(3)
+    n = 8
+    b = 1.0 + 2.0 ** -30
+    v = b + rng.uniform(-1e-9, 1e-9, (n + 1,) * 3)
+    bounds = (b - 1.0, b)
+    tf = glue.color_tf_from_layers(bounds, 256, testing.ctf_layers(bounds, 4))
+    out = {"vertex": v, "tf_y": np.array([t.y for t in tf.tables]), "tf_bounds": np.array(bounds)}
+    dims = np.array([n, n, n], dtype=np.int64)
+    for ci, (pos, width, res, lens) in enumerate(NB_CAMS):
+        for ns in (1, 3):
+            cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+            p = cam.sampler_params()
+            s = RIS.VolumeRenderSampler(*sampler_args(p), tf, ns, lens_type=p["lens_type"],
+                                        camera_data=p["camera_data"], zbuffer=np.ones(res))
+            s(PartitionedGrid(0, [v], np.ones((n, n, n), "uint8"), np.zeros(3), np.ones(3), dims), num_threads=1)
+            out[f"img_{ci}_{ns}"] = np.array(s.aimage)
+    np.savez_compressed(HERE / "near_bound.npz", **out)
 
 
 LIGHTS = [((1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 1.0)), ((-0.3, 0.8, 0.2), (0.9, 0.5, 0.2, 1.0))]
@@ -332,7 +363,7 @@ def offaxis():
 
 
 ALL = {"gz": gz, "trace": trace, "vr": vr, "light": light, "octree": octree, "proj": proj, "kd": kd_and_amr,
-       "offaxis": offaxis}
+       "offaxis": offaxis, "near_bound": near_bound}
 
 if __name__ == "__main__":
     for name in sys.argv[1:] or list(ALL):

@@ -252,6 +252,27 @@ def test_range_decisions_near_a_bound(emu, which, kind, ns):
         assert relative_error(f32, ref, channels=chans)[0] > 1e-2
 
 
+@pytest.mark.parametrize("ci", range(2))
+@pytest.mark.parametrize("ns", [1, 3])
+def test_range_decisions_match_yt(emu, ci, ns):
+    """Against yt's own images of the near-bound field (near_bound.npz, from
+    yt's compiled VolumeRenderSampler): the kernel's walk with the float64
+    range decisions within 1e-5, without them far off."""
+    from test_oracle_golden import NB_CAMS, GoldenTF
+
+    f = np.load(ROOT / "tests" / "golden" / "near_bound.npz")
+    tf = GoldenTF(f["tf_bounds"], f["tf_y"])
+    pos, width, res, lens = NB_CAMS[ci]
+    cam = Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+    n = f["vertex"].shape[0] - 1
+    bricks = [([f["vertex"]], None, np.zeros(3), np.ones(3), np.array([n, n, n]))]
+    ref = f[f"img_{ci}_{ns}"]
+    img, *_ = run_emu(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf, ns, with_lo=True)
+    assert relative_error(img, ref, channels=(0, 1, 2))[0] <= TOL
+    f32, *_ = run_emu(emu, bricks, cam, np.array([0]), _lib.VOLUME_RENDER, tf, ns, with_lo=False)
+    assert relative_error(f32, ref, channels=(0, 1, 2))[0] > 1e-2
+
+
 def test_range_decision_tolerance_covers_float32_error(emu):
     """The tolerance (range_tol) bounds the float32 sample value's error:
     on AMR bricks with a transfer function whose bounds cut through the

@@ -59,6 +59,26 @@ def test_walk_volume_trace_exact():
         assert np.array_equal(ts[i, :n].view(np.uint64), f["ts"][i, :n].view(np.uint64)), i
 
 
+NB_CAMS = [((0.3, 0.6, -1.0), (1.5, 1.5, 1.5), (24, 24), "perspective"),
+           ((1.2, 0.3, -0.8), (1.0, 1.0, 1.0), (20, 24), "plane-parallel")]
+
+
+@pytest.mark.parametrize("ci", range(2))
+@pytest.mark.parametrize("ns", [1, 3])
+def test_near_bound_exact(ci, ns):
+    """yt's float64 range test on a field within 1e-9 of a transfer-function
+    bound (near_bound.npz): the oracle keeps and drops the same samples."""
+    f = load("near_bound.npz")
+    tf = GoldenTF(f["tf_bounds"], f["tf_y"])
+    pos, width, res, lens = NB_CAMS[ci]
+    cam = glue.Camera(pos, (0.5, 0.5, 0.5), width, res, lens_type=lens)
+    n = f["vertex"].shape[0] - 1
+    brick = ([f["vertex"]], None, np.zeros(3), np.ones(3), [n, n, n])
+    img, visits = glue.render("volume_render", cam, [brick], None, tf=tf, n_samples=ns)
+    assert visits > 0
+    assert np.array_equal(img, f[f"img_{ci}_{ns}"])
+
+
 @pytest.mark.parametrize("ci", range(3))
 @pytest.mark.parametrize("ns", [1, 3])
 def test_volume_render_exact(ci, ns):
