@@ -34,9 +34,11 @@ tests do not depend on the synthetic generators staying bit-stable.
 * near_bound.npz VolumeRenderSampler on a field within 1e-9 of a
                 transfer-function bound float32 cannot represent (the
                 float64 range decisions), two cameras, 1 and 3 samples
+* amr_cut.npz   the amr_vr.npz render under three ColorTransferFunctions
+                whose bounds cut through the data
 
-Pass fixture names (gz trace vr light octree proj kd offaxis near_bound) to
-make only those.
+Pass fixture names (gz trace vr light octree proj kd offaxis near_bound
+amr_cut) to make only those.
 """
 from __future__ import annotations
 
@@ -313,6 +315,42 @@ def kd_and_amr():
                         tf_bounds=np.array(bounds), viewpoint=cam.viewpoint)
 
 
+AMR_CUT_BOUNDS = [(0.05, 0.55), (0.25, 0.95), (-0.1, 0.4)]
+
+
+def amr_cut():
+    """The amr_vr.npz render with ColorTransferFunctions whose bounds cut
+    through the data (the served form's kind: samples at the bounds are
+    common, the brightest layer 1/60 of the range from the upper bound)."""
+    grids = testing.amr_blob_grids(root=16, levels=2, patch=8, seed=3)
+    gles = np.array([g.left_edge for g in grids])
+    gres = np.array([g.right_edge for g in grids])
+    gids = np.array([g.id for g in grids], dtype=np.int64)
+    levels = np.array([g.level for g in grids], dtype=np.int32)
+    trunk = ref_tree(gles, gres, gids, levels)
+    vcd = {g.id: np.log10(ref_vertex(g.data)) for g in grids}
+    byid = {g.id: g for g in grids}
+    cam = glue.Camera((0.3, 0.6, -1.1), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), (32, 28), lens_type="perspective")
+    out = {"viewpoint": cam.viewpoint}
+    for k, bounds in enumerate(AMR_CUT_BOUNDS):
+        tf = glue.color_tf_from_layers(bounds, 128, testing.ctf_layers(bounds, 6))
+        p = cam.sampler_params()  # (a new image for each render)
+        s = RIS.VolumeRenderSampler(*sampler_args(p), tf, 1, lens_type=p["lens_type"], camera_data=p["camera_data"],
+                                    zbuffer=np.ones((32, 28)))
+        for node in trunk.kd_traverse(viewpoint=cam.viewpoint):
+            g = byid[node.grid]
+            nle, nre = node.get_left_edge(), node.get_right_edge()
+            li = np.rint((nle - g.left_edge) / g.dds).astype("int32")
+            ri = np.rint((nre - g.left_edge) / g.dds).astype("int32")
+            dims = (ri - li).astype("int64")
+            d = vcd[g.id][li[0]: ri[0] + 1, li[1]: ri[1] + 1, li[2]: ri[2] + 1].copy()
+            s(PartitionedGrid(g.id, [d], np.ones(dims, "uint8"), nle, nre, dims), num_threads=1)
+        out[f"image_{k}"] = np.array(s.aimage)
+        out[f"tf_y_{k}"] = np.array([t.y for t in tf.tables])
+        out[f"tf_bounds_{k}"] = np.array(bounds)
+    np.savez_compressed(HERE / "amr_cut.npz", **out)
+
+
 def offaxis_cases():
     """Inputs of offaxis.npz: the cells of a small octree (levels 2-5) seen
     along oblique normals on square, non-square (Nx < Ny), one- and
@@ -363,7 +401,7 @@ def offaxis():
 
 
 ALL = {"gz": gz, "trace": trace, "vr": vr, "light": light, "octree": octree, "proj": proj, "kd": kd_and_amr,
-       "offaxis": offaxis, "near_bound": near_bound}
+       "offaxis": offaxis, "near_bound": near_bound, "amr_cut": amr_cut}
 
 if __name__ == "__main__":
     for name in sys.argv[1:] or list(ALL):

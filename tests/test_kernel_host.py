@@ -273,6 +273,22 @@ def test_range_decisions_match_yt(emu, ci, ns):
     assert relative_error(f32, ref, channels=(0, 1, 2))[0] > 1e-2
 
 
+@pytest.mark.parametrize("k", range(3))
+def test_amr_cut_bounds_match_yt(emu, k):
+    """yt's own AMR renders under transfer functions whose bounds cut through
+    the data (amr_cut.npz): the kernel's walk with float64 range decisions
+    within 1e-5."""
+    from test_oracle_golden import GoldenTF, amr_cut_bricks
+
+    g = np.load(ROOT / "tests" / "golden" / "amr_cut.npz")
+    bricks, gcam = amr_cut_bricks()
+    cam = Camera((0.3, 0.6, -1.1), (0.5, 0.5, 0.5), (1.5, 1.5, 1.5), (32, 28), lens_type="perspective")
+    assert np.array_equal(cam.viewpoint, gcam.viewpoint)
+    tf = GoldenTF(g[f"tf_bounds_{k}"], g[f"tf_y_{k}"])
+    img, *_ = run_emu(emu, bricks, cam, np.arange(len(bricks)), _lib.VOLUME_RENDER, tf, with_lo=True)
+    assert relative_error(img, g[f"image_{k}"], channels=(0, 1, 2))[0] <= TOL
+
+
 def test_range_decision_tolerance_covers_float32_error(emu):
     """The tolerance (range_tol) bounds the float32 sample value's error:
     on AMR bricks with a transfer function whose bounds cut through the
