@@ -201,6 +201,26 @@ def test_degenerate_images(emu, res, lens):
     assert np.allclose(img[ok], ref[ok], rtol=1e-5, atol=1e-12)
 
 
+@pytest.mark.parametrize("kind", [_lib.PROJECTION, _lib.MIP, _lib.INTERPOLATED_PROJECTION])
+@pytest.mark.parametrize("nf", [2, 4, 5])
+def test_multi_field_projections(emu, kind, nf):
+    """Bricks of several fields: the projection samplers write min(nf, 4)
+    channels (interpolated projection min(nf, 3)), through the cell loop
+    that reads the channel count from the brick (one-field bricks take the
+    loop compiled for one channel)."""
+    grids = testing.amr_blob_grids(root=16, levels=2, patch=8, seed=4)
+    kd = AMRKDTree(grids, log_field=False)
+    vertex = kind == _lib.INTERPOLATED_PROJECTION
+    bricks = []
+    for d, m, le, re, dims in kd.bricks():
+        base = d[0] if vertex else d[0][:-1, :-1, :-1].copy()
+        bricks.append(([base * (1.0 + 0.25 * k) + k for k in range(nf)], m, le, re, dims))
+    cam = Camera((1.2, 0.35, -0.8), 0.5, 1.2, 24, lens_type="perspective")
+    order = kd.viewpoint_order(cam.viewpoint)
+    chans = tuple(range(min(nf, 3 if vertex else 4)))
+    check(emu, bricks, cam, order, kind, channels=chans)
+
+
 def test_empty_brick_list(emu):
     """No bricks in the order: no walk, the image as it was."""
     w = workloads.uniform_vr(n=8, res=8)
