@@ -240,15 +240,18 @@ def near_bound_case(n=8, seed=3):
     v = b + rng.uniform(-1e-9, 1e-9, (n + 1,) * 3)
     bricks = [([v], None, np.zeros(3), np.ones(3), np.array([n, n, n]))]
     ctf = workloads.color_tf((b - 1.0, b), 4)
+    grey = workloads.color_tf((b - 1.0, b), 4)
+    grey.grey_opacity = True
     tf = TransferFunction((b - 1.0, b), 64)
     tf.add_gaussian(b - 0.02, 0.01, 1.0)
     mv = MultiVariateTransferFunction()
     mv.add_field_table(tf, 0)
     mv.link_channels(0, [0, 1, 2, 3])
-    return bricks, {"ctf": ctf, "general": mv}
+    return bricks, {"ctf": ctf, "grey": grey, "general": mv}
 
 
 @pytest.mark.parametrize("which,kind,ns", [("ctf", _lib.VOLUME_RENDER, 1), ("ctf", _lib.VOLUME_RENDER, 3),
+                                           ("grey", _lib.VOLUME_RENDER, 1), ("grey", _lib.VOLUME_RENDER, 2),
                                            ("general", _lib.VOLUME_RENDER, 1),
                                            ("ctf", _lib.LIGHT_SOURCE, 2)])
 def test_range_decisions_near_a_bound(emu, which, kind, ns):
